@@ -1,0 +1,191 @@
+/*
+ * s2kit_gb300.h -- C ABI of the GB300 (sm_103a) seminaive spherical harmonic transform library.
+ *
+ * Part 1 is a drop-in for S2kit 1.1's memo path: every function keeps the reference
+ * signature (include/s2kit/*.h), argument meaning and coefficient layout, takes HOST
+ * buffers, and runs on the GPU (CUDA device 0 unless S2G_DEVICE selects another).
+ * FFTW plans are accepted and ignored (NULL is fine).  Tables produced by the table
+ * builders below are generated on the GPU and copied into the caller's buffers.
+ *
+ * Part 2 adds status-returning entry points on DEVICE pointers, batched over functions,
+ * with an explicit CUDA stream, and a split-precision (tensor core) real-field path.
+ *
+ * Coefficient layout (both parts): f(m,l) at IndexOfHarmonicCoeff(m,l,bw), real and
+ * imaginary parts in separate arrays of bw*bw doubles (util.c:42-49).
+ * Sample layout: (2bw)^2 values, latitude-major [theta_j][phi_k],
+ * theta_j = pi (2j+1) / (4bw), phi_k = 2 pi k / (2bw).
+ */
+#ifndef S2KIT_GB300_H
+#define S2KIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* include/s2kit/util.h:16-19 */
+#ifndef _UTIL_H
+typedef enum {
+    COMPLEX = 0, /* data is complex */
+    REAL         /* data is real */
+} DataFormat;
+#endif
+
+/* FFTW plan handle as seen by the reference signatures.  When <fftw3.h> is included
+ * first its own definition is used; the library never dereferences plans. */
+#ifndef FFTW3_H
+typedef struct fftw_plan_s* fftw_plan;
+#endif
+
+/* =============================== Part 1: drop-in ================================ */
+
+/* Replaces FSTSemiMemo, src/FST_semi_memo.c:68-202 (include/s2kit/FST_semi_memo.h:8-9).
+ * The table argument is uploaded on first use and cached by address (see
+ * s2g_cache_clear); workspace, plans and weights are not needed (device copies). */
+void FSTSemiMemo(double* rdata, double* idata, double* rcoeffs, double* icoeffs, const int bw,
+                 double** seminaive_naive_table, double* workspace, DataFormat data_format, const int cutoff,
+                 fftw_plan* DCT_plan, fftw_plan* FFT_plan, double* weights);
+
+/* Replaces InvFSTSemiMemo, src/FST_semi_memo.c:228-351 (FST_semi_memo.h:11-12). */
+void InvFSTSemiMemo(double* rcoeffs, double* icoeffs, double* rdata, double* idata, const int bw,
+                    double** transpose_seminaive_naive_table, double* workspace, DataFormat data_format,
+                    const int cutoff, fftw_plan* inv_DCT_plan, fftw_plan* inv_FFT_plan);
+
+/* Replaces FZTSemiMemo, src/FST_semi_memo.c:374-407 (FST_semi_memo.h:14).  As in the
+ * reference, REAL data writes 2*bw zeros to ires. */
+void FZTSemiMemo(double* rdata, double* idata, double* rres, double* ires, const int bw, double* cos_pml_table,
+                 double* workspace, DataFormat data_format, fftw_plan* DCT_plan, double* weights);
+
+/* Replaces ConvOn2SphereSemiMemo, src/FST_semi_memo.c:439-518 (FST_semi_memo.h:16).
+ * Device tables for bw are generated once and cached (the reference rebuilds them
+ * on every call); workspace is unused. */
+void ConvOn2SphereSemiMemo(double* rdata, double* idata, double* rfilter, double* ifilter, double* rres,
+                           double* ires, const int bw, double* workspace);
+
+/* Replaces DLTSemi, src/legendre_transform/seminaive.c:153-198 (seminaive.h:6). */
+void DLTSemi(double* data, const int bw, const int m, double* result, double* workspace, double* cos_pml_table,
+             double* weights, fftw_plan* plan);
+
+/* Replaces InvDLTSemi, src/legendre_transform/seminaive.c:56-115 (seminaive.h:8). */
+void InvDLTSemi(double* coeffs, const int bw, const int m, double* result, double* trans_cos_pml_table,
+                double* sin_values, double* workspace, fftw_plan* plan);
+
+/* Replace DLTNaive / InvDLTNaive, src/legendre_transform/naive.c:34-59, 78-96 (naive.h:4-6). */
+void DLTNaive(double* data, const int bw, const int m, double* weights, double* result, double* pml_table,
+              double* workspace);
+void InvDLTNaive(double* coeffs, const int bw, const int m, double* result, double* pml_table);
+
+/* Replaces GenerateWeightsForDLT, src/legendre_transform/weights.c:32-47 (weights.h:4). */
+void GenerateWeightsForDLT(const int bw, double* weights);
+
+/* Table builders, src/legendre_polynomials/cospml.c and pml.c (cospml.h:6-30, pml.h:4). */
+void GenerateCosPmlTable(const int bw, const int m, double* tablespace, double* workspace); /* cospml.c:161-242 */
+void TransposeCosPmlTable(const int bw, const int m, double* cos_pml_table, double* result); /* cospml.c:301-362 */
+double** Spharmonic_Pml_Table(const int bw, double* resultspace, double* workspace);     /* cospml.c:387-401 */
+double** Transpose_Spharmonic_Pml_Table(double** spharmonic_pml_table, const int bw,
+                                        double* resultspace);                                /* cospml.c:415-428 */
+double** SemiNaive_Naive_Pml_Table(const int bw, const int m, double* resultspace,
+                                   double* workspace);                                        /* cospml.c:451-475 */
+double** Transpose_SemiNaive_Naive_Pml_Table(double** seminaive_naive_pml_table, const int bw, const int m,
+                                             double* resultspace, double* workspace);        /* cospml.c:490-518 */
+void GeneratePmlTable(const int bw, const int m, double* pml_table, double* workspace);     /* pml.c:41-79 */
+void Pmm_L2(const int m, double* eval_points, const int n, double* result);                /* pmm.c:21-34 */
+
+/* Size / layout helpers (integer arithmetic only), cospml.c:39-288. */
+int TableSize(const int m, const int bw);                    /* cospml.c:39-59 */
+int Spharmonic_TableSize(const int bw);                      /* cospml.c:85-92 */
+int Reduced_SpharmonicTableSize(const int bw, const int m);  /* cospml.c:107-115 */
+int Reduced_Naive_TableSize(const int bw, const int m);      /* cospml.c:434-440 */
+int TableOffset(int m, int l);                               /* cospml.c:123-134 */
+int RowSize(const int m, const int l);                       /* cospml.c:250-258 */
+int Transpose_RowSize(const int row, const int m, const int bw); /* cospml.c:270-288 */
+
+/* src/util/util.c:42-49 and :68-103 (util.h:15-17) */
+int IndexOfHarmonicCoeff(const int m, const int l, const int bw);
+void TransMult(double* rdatacoeffs, double* idatacoeffs, double* rfiltercoeffs, double* ifiltercoeffs,
+               double* rres, double* ires, const int bw);
+
+/* src/util/chebyshev_nodes.c:15-34 (chebyshev_nodes.h:4-6) */
+void AcosOfChebyshevNodes(const int n, double* eval_points);
+void ChebyshevNodes(const int n, double* eval_points);
+
+/* ============================ Part 2: device API ================================== */
+
+typedef enum {
+    S2G_OK = 0,
+    S2G_ERR_ARG = 1,         /* invalid argument (bw, cutoff, batch, NULL pointer, precision) */
+    S2G_ERR_NOMEM = 2,       /* device or host allocation failed */
+    S2G_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    S2G_ERR_UNSUPPORTED = 4, /* valid request this build does not implement (e.g. odd bw on tensor cores) */
+    S2G_ERR_TIMEOUT = 5,     /* a bounded device-side wait expired */
+    S2G_ERR_NOGPU = 6        /* no usable CUDA device */
+} s2g_status;
+
+typedef enum {
+    S2G_PREC_FP64 = 0,   /* plain FP64 everywhere (parity path) */
+    S2G_PREC_BF16X3 = 1, /* FP32 FFT/DCT, Legendre contraction as 3-term split BF16 on tcgen05, FP32 accumulate */
+    S2G_PREC_BF16X2 = 2  /* as above with 2-term splits (3 products) */
+} s2g_precision;
+
+/* Last error message of the calling thread ("" if none). */
+const char* s2g_last_error(void);
+/* Library version string. */
+const char* s2g_version(void);
+/* Drops every cached device table and uploaded caller table (all devices). */
+int s2g_cache_clear(void);
+
+typedef struct s2g_plan_s* s2g_plan;
+
+/* Creates a plan for bandwidth bw (even, 2 <= bw <= 4096 for FP64; odd bw up to 255) and a
+ * seminaive/naive cutoff (1 <= cutoff <= bw).  Tables are generated on the current device
+ * (FP64 recurrence and DCT, cospml.c:161-242) and shared by every plan with the same
+ * (device, bw, cutoff). */
+int s2g_plan_create(s2g_plan* plan, int bw, int cutoff);
+int s2g_plan_destroy(s2g_plan plan);
+/* Device bytes of scratch a call with this batch needs (the plan grows its own scratch
+ * on demand when the caller passes none). */
+size_t s2g_plan_workspace_size(s2g_plan plan, int batch, int precision);
+
+/* Batched FP64 transforms on device pointers.  Function f of the batch uses
+ * rdata + f*(2bw)^2 and rcoeffs + f*bw*bw (likewise for the imaginary arrays).
+ * REAL with idata == NULL (forward) or idata == NULL (inverse output) selects the
+ * real-field fast path (imaginary samples taken as zero / not written).  `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  Asynchronous with respect to the host. */
+int s2g_fst(s2g_plan plan, const double* rdata, const double* idata, double* rcoeffs, double* icoeffs, int batch,
+            DataFormat data_format, void* stream);
+int s2g_inv_fst(s2g_plan plan, const double* rcoeffs, const double* icoeffs, double* rdata, double* idata,
+                int batch, DataFormat data_format, void* stream);
+/* Zonal transform of `batch` functions: rres/ires hold bw (COMPLEX) values per function;
+ * REAL zeroes 2*bw imaginary values per function as the reference does. */
+int s2g_fzt(s2g_plan plan, const double* rdata, const double* idata, double* rres, double* ires, int batch,
+            DataFormat data_format, void* stream);
+/* Coefficient-space product with a zonal filter (TransMult), batched. */
+int s2g_transmult(int bw, const double* rdatacoeffs, const double* idatacoeffs, const double* rfiltercoeffs,
+                  const double* ifiltercoeffs, double* rres, double* ires, int batch, void* stream);
+/* Convolution of `batch` real functions with one zonal filter (ConvOn2SphereSemiMemo),
+ * plan must have cutoff == bw. */
+int s2g_conv(s2g_plan plan, const double* rdata, const double* idata, const double* rfilter,
+             const double* ifilter, double* rres, double* ires, int batch, void* stream);
+
+/* Real-field batched transforms with FP32 samples/coefficients and a selectable
+ * precision for the Legendre contraction (s2g_precision).  grid: batch*(2bw)^2 floats;
+ * rcoeffs/icoeffs: batch*bw*bw floats in the reference layout, negative orders filled by
+ * f(l,-m) = (-1)^m conj f(l,m) on output and ignored on input. */
+int s2g_fst_real_f32(s2g_plan plan, const float* grid, float* rcoeffs, float* icoeffs, int batch, int precision,
+                     void* stream);
+int s2g_inv_fst_real_f32(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid, int batch,
+                         int precision, void* stream);
+
+/* Same on HOST buffers: copies in, transforms, copies out (chunked, copies overlapped with
+ * compute on the plan's streams); returns when the results are in host memory. */
+int s2g_fst_real_f32_host(s2g_plan plan, const float* grid, float* rcoeffs, float* icoeffs, int batch,
+                          int precision);
+int s2g_inv_fst_real_f32_host(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid, int batch,
+                              int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* S2KIT_GB300_H */

@@ -1,0 +1,186 @@
+// s2g_common.cuh -- shared device helpers for the GB300 seminaive SHT library.
+//
+// Block-cooperative transforms in shared memory with FFTW's documented conventions
+// (the reference S2kit calls FFTW3 for these; FST_semi_memo.c:81,350, seminaive.c:107,170,
+// cospml.c:203-224):
+//   DFT sign -1 : X[k] = sum_j x[j] exp(-2 pi i j k / n)     (unnormalised)
+//   REDFT10     : Y[k] = 2 sum_j x[j] cos(pi (j+1/2) k / n)  (DCT-II)
+//   REDFT01     : Y[k] = x[0] + 2 sum_{j>=1} x[j] cos(pi j (k+1/2) / n)  (DCT-III)
+// Power-of-two lengths use an in-place radix-2 decimation-in-time FFT whose input is
+// stored in bit-reversed order; other lengths use a direct O(n^2) DFT.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace s2g {
+
+// ---------------------------------------------------------------------------------
+// Geometry of one transform length n.
+struct Len {
+    int n;      // length
+    int logn;   // log2(n) when n is a power of two, else -1
+    __host__ __device__ bool pow2() const { return logn >= 0; }
+    // position at which input element k must be stored before block_dft()
+    __device__ __forceinline__ int pos(int k) const {
+        return logn > 0 ? (int)(__brev((unsigned)k) >> (32 - logn)) : k;
+    }
+};
+
+inline Len make_len(int n) {
+    int lg = -1;
+    if (n > 0 && (n & (n - 1)) == 0) {
+        lg = 0;
+        while ((1 << lg) < n) ++lg;
+    }
+    return Len{n, lg};
+}
+
+// ---------------------------------------------------------------------------------
+// In-place DFT of `cnt` sequences re/im[s*stride + k], k < L.n (input in L.pos order).
+// tw[k] = (cos(2 pi k / n), sin(2 pi k / n)) for k < n.  Ends with __syncthreads().
+// For non power-of-two n, `tmp` must hold 2*n reals (used one sequence at a time).
+template <typename T, typename T2>
+__device__ void block_dft(T* re, T* im, Len L, int cnt, int stride, const T2* __restrict__ tw, T sign,
+                          T* tmp) {
+    const int n = L.n;
+    if (L.pow2()) {
+        const int hn = n >> 1;
+        const int total = cnt * hn;
+        const int lhn = L.logn - 1;
+        for (int s = 1; s <= L.logn; ++s) {
+            const int half = 1 << (s - 1);
+            const int tshift = L.logn - s;  // twiddle index = j * (n / len)
+            for (int t = threadIdx.x; t < total; t += blockDim.x) {
+                const int seq = t >> lhn;
+                const int b = t & (hn - 1);
+                const int j = b & (half - 1);
+                const int a0 = ((b >> (s - 1)) << s) + j;
+                const int a1 = a0 + half;
+                const T2 w = tw[j << tshift];
+                const T c = w.x, sn = sign * w.y;
+                T* r = re + (size_t)seq * stride;
+                T* i = im + (size_t)seq * stride;
+                const T xr = r[a1] * c - i[a1] * sn;
+                const T xi = r[a1] * sn + i[a1] * c;
+                const T yr = r[a0], yi = i[a0];
+                r[a1] = yr - xr;
+                i[a1] = yi - xi;
+                r[a0] = yr + xr;
+                i[a0] = yi + xi;
+            }
+            __syncthreads();
+        }
+        return;
+    }
+    for (int seq = 0; seq < cnt; ++seq) {
+        T* r = re + (size_t)seq * stride;
+        T* i = im + (size_t)seq * stride;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            T sr = 0, si = 0;
+            int idx = 0;
+            for (int j = 0; j < n; ++j) {
+                const T2 w = tw[idx];
+                const T c = w.x, sn = sign * w.y;
+                sr += r[j] * c - i[j] * sn;
+                si += r[j] * sn + i[j] * c;
+                idx += k;
+                if (idx >= n) idx -= n;
+            }
+            tmp[k] = sr;
+            tmp[n + k] = si;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            r[k] = tmp[k];
+            i[k] = tmp[n + k];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Block-wide exclusive prefix sum of v[0..n) (int), in place; `warp_tot` needs 32 ints.
+// Ends with __syncthreads().
+__device__ inline void block_exclusive_scan(int* v, int n, int* warp_tot) {
+    // serial chunks per thread, then a scan over thread totals via warps
+    const int nt = blockDim.x;
+    const int per = (n + nt - 1) / nt;
+    const int lo = threadIdx.x * per;
+    const int hi = min(n, lo + per);
+    int s = 0;
+    for (int k = lo; k < hi; ++k) s += v[k];
+    // inclusive warp scan of s
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = (nt + 31) >> 5;
+        int t = lane < nw ? warp_tot[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) warp_tot[lane] = t;
+    }
+    __syncthreads();
+    int base = (wid ? warp_tot[wid - 1] : 0) + x - s;  // exclusive prefix of this thread's chunk
+    for (int k = lo; k < hi; ++k) {
+        int t = v[k];
+        v[k] = base;
+        base += t;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------------
+// Index helpers (device copies of the reference's integer formulas).
+
+// util.c:42-49
+__host__ __device__ __forceinline__ int index_of_harmonic_coeff(int m, int l, int bw) {
+    const int L = bw - 1;
+    if (m >= 0) return m * bw - (m * (m - 1)) / 2 + (l - m);
+    const int am = -m;
+    return (L * (L + 3)) / 2 + 1 + ((L - am) * (L - am + 1)) / 2 + (l - am);
+}
+
+// cospml.c:250-258
+__host__ __device__ __forceinline__ int row_size(int m, int l) {
+    if (l < m) return 0;
+    return (m % 2 == 0) ? (l / 2) + 1 : ((l - 1) / 2) + 1;
+}
+
+__host__ __device__ __forceinline__ int64_t prefix_even(int64_t n) {
+    if (n <= 0) return 0;
+    const int64_t q = n / 2, r = n % 2;
+    return q * (q - 1) + r * q + n;
+}
+
+// cospml.c:123-134 (offset of row l inside the order-m table)
+__host__ __device__ __forceinline__ int64_t table_offset(int m, int l) {
+    if (m % 2 == 0) return prefix_even(l) - prefix_even(m);
+    return prefix_even(l - 1) - prefix_even(m - 1);
+}
+
+// cospml.c:39-59
+__host__ __device__ __forceinline__ int64_t table_size(int m, int bw) { return table_offset(m, bw); }
+
+// First degree l whose cosine series contains frequency `row` (transposed table row).
+__host__ __device__ __forceinline__ int trans_first_l(int row, int m) {
+    return (row > m) ? row + (m % 2) : m + (row % 2);
+}
+
+// cospml.c:270-288 (true count; equals the reference for even bandwidths)
+__host__ __device__ __forceinline__ int transpose_row_size(int row, int m, int bw) {
+    if (row >= bw) return 0;
+    const int l0 = trans_first_l(row, m);
+    if (l0 >= bw) return 0;
+    return (bw - l0 + 1) / 2;
+}
+
+}  // namespace s2g

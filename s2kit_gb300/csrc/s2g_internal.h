@@ -1,0 +1,101 @@
+// s2g_internal.h -- internal (non-exported) declarations of the GB300 seminaive SHT library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/s2kit_gb300.h"
+
+namespace s2g {
+
+// Records a formatted message for s2g_last_error() and returns `code`.
+int fail(int code, const char* fmt, ...);
+// cudaError_t -> status (records the CUDA error string)
+int cuda_fail(cudaError_t e, const char* what);
+
+#define S2G_CUDA(call)                                           \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return ::s2g::cuda_fail(e_, #call); \
+    } while (0)
+
+#define S2G_TRY(call)            \
+    do {                         \
+        int r_ = (call);         \
+        if (r_ != S2G_OK) return r_; \
+    } while (0)
+
+// Device tables and constants for one (bandwidth, cutoff) on one device.
+struct Tables {
+    int bw = 0, cutoff = 0, device = -1;
+    int64_t total = 0;          // doubles in each of fwd / inv
+    double* fwd = nullptr;      // reference layout: SemiNaive_Naive_Pml_Table (cospml.c:451-475)
+    double* inv = nullptr;      // Transpose_SemiNaive_Naive_Pml_Table layout (cospml.c:490-518)
+    int64_t* off = nullptr;     // bw offsets (device)
+    int64_t* h_off = nullptr;   // same, host copy
+    double* weights = nullptr;  // 4*bw (weights.c:32-47)
+    double* sinv = nullptr;     // sin(theta_j), 2*bw
+    double2* tw_S = nullptr;    // exp(2 pi i k / 2bw), k < 2bw   (cos, sin)
+    double2* tw_D = nullptr;    // exp(i pi k / (2 * 2bw)), k < 2bw (DCT pre/post twiddle)
+    // split-precision (tensor core) operands, built on first use
+    void* split = nullptr;
+};
+
+// Device scratch owned by a plan; grown on demand.
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need);
+    void release();
+};
+
+// Build / fetch device tables (cached per device, bw, cutoff).
+int get_tables(int bw, int cutoff, Tables** out);
+// Build tables into caller-visible device buffers (used by the host table builders).
+int build_tables(Tables* t, cudaStream_t st);
+int generate_weights_device(int bw, double* d_weights, cudaStream_t st);
+int generate_cos_pml_device(int bw, int m_begin, int m_end, double* d_fwd, const int64_t* d_off,
+                            cudaStream_t st);
+int transpose_cos_pml_device(int bw, int m_begin, int m_end, const double* d_fwd, double* d_inv,
+                             const int64_t* d_off, cudaStream_t st);
+int generate_pml_device(int bw, int m_begin, int m_end, double* d_fwd, const int64_t* d_off, cudaStream_t st);
+int pmm_device(int m, const double* d_eval, int n, double* d_out, cudaStream_t st);
+int nodes_device(int n, double* d_out, int acos_only, cudaStream_t st);
+
+// ---- FP64 pipeline (sht_fp64.cu) ----
+struct F64Work {
+    double* Xr;  // [batch][rows][2bw]
+    double* Xi;
+    int rows;    // rows per function in X (bw for REAL, 2bw for COMPLEX)
+};
+size_t f64_work_bytes(int bw, int batch, int data_format);
+int fst_f64(const Tables* t, const double* rdata, const double* idata, double* rc, double* ic, int batch,
+            int data_format, int cutoff, void* work, cudaStream_t st);
+int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rdata, double* idata, int batch,
+                int data_format, int cutoff, void* work, cudaStream_t st);
+int fzt_f64(const Tables* t, const double* rdata, const double* idata, double* rres, double* ires, int batch,
+            int data_format, void* work, cudaStream_t st);
+int transmult_f64(const double* rd, const double* id, const double* rf, const double* iff, double* rr,
+                  double* ir, int bw, int batch, cudaStream_t st);
+// 1-D transforms with caller-provided (device) tables for a single order m
+int dlt_semi_f64(const double* data, int bw, int m, double* result, const double* table, const double* weights,
+                 const double2* tw_S, const double2* tw_D, cudaStream_t st);
+int inv_dlt_semi_f64(const double* coeffs, int bw, int m, double* result, const double* ttable,
+                     const double* sinv, const double2* tw_S, const double2* tw_D, cudaStream_t st);
+int dlt_naive_f64(const double* data, int bw, int m, const double* weights, double* result, const double* ptable,
+                  cudaStream_t st);
+int inv_dlt_naive_f64(const double* coeffs, int bw, int m, double* result, const double* ptable,
+                      cudaStream_t st);
+int twiddles_device(int n, double2* d_tw_full, double2* d_tw_quarter, cudaStream_t st);
+
+// ---- split-precision pipeline (sht_split.cu) ----
+size_t split_work_bytes(int bw, int batch);
+int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int precision, void* work,
+              cudaStream_t st);
+int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int batch, int precision, void* work,
+                  cudaStream_t st);
+
+}  // namespace s2g

@@ -1,0 +1,822 @@
+// sht_fp64.cu -- plain FP64 seminaive SHT on the GPU (the parity path).
+//
+// Forward (FSTSemiMemo, FST_semi_memo.c:68-202):
+//   k_rows_fwd : DFT along phi of every latitude row, scaled by sqrt(2 pi)/2bw and stored
+//                transposed X[f][m][theta]          (FST_semi_memo.c:81-90)
+//   k_fwd_dlt  : per (order row, group of functions): weights, REDFT10 of length 2bw,
+//                normalisation, then the seminaive triangular contraction against the
+//                cosine-series table (DLTSemi, seminaive.c:153-198) or, for orders >= cutoff,
+//                the naive sampled-Pml product (DLTNaive, naive.c:34-59); writes the
+//                coefficients at IndexOfHarmonicCoeff positions (+ REAL mirror, :131-145)
+// Inverse (InvFSTSemiMemo, FST_semi_memo.c:228-351):
+//   k_inv_dlt  : per (order row, group): transposed contraction (InvDLTSemi, seminaive.c:56-115)
+//                or naive synthesis (InvDLTNaive, naive.c:78-96), REDFT01, sin(theta) for odd m,
+//                sign for odd negative rows, 1/sqrt(2 pi)  -> Fourier rows F[f][m][theta]
+//   k_rows_inv : per latitude, DFT with sign +1 over m (the reference's swapped re/im forward
+//                DFT, FST_semi_memo.c:350) -> samples
+// The real-field fast path (no imaginary samples) packs two latitudes into one complex DFT.
+#include <math.h>
+
+#include "s2g_common.cuh"
+#include "s2g_internal.h"
+
+namespace s2g {
+
+static constexpr double kPi = 3.14159265358979323846;
+static constexpr double kSqrtHalf = 0.70710678118654752440;
+
+// ------------------------------------------------------------------------------------
+__global__ void k_twiddles(int n, double2* full, double2* quarter) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double s, c;
+    if (full) {
+        sincospi(2.0 * (double)k / (double)n, &s, &c);
+        full[k] = make_double2(c, s);
+    }
+    if (quarter) {
+        sincospi((double)k / (2.0 * (double)n), &s, &c);
+        quarter[k] = make_double2(c, s);
+    }
+}
+
+int twiddles_device(int n, double2* d_full, double2* d_quarter, cudaStream_t st) {
+    k_twiddles<<<(n + 255) / 256, 256, 0, st>>>(n, d_full, d_quarter);
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+static int set_smem(const void* fn, size_t bytes) {
+    if (bytes > 48 * 1024) S2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return S2G_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Row DFTs along phi.  One CTA: R complex sequences of length S.
+//   complex mode (idata != null): sequence r = latitude j0 + r
+//   real mode    (idata == null): sequence r = latitudes j0 + 2r (real part), j0 + 2r + 1 (imag part)
+// Output X[f][m][theta] for m < rows_out, scaled.
+__global__ void k_rows_fwd(const double* __restrict__ rdata, const double* __restrict__ idata,
+                           double* __restrict__ Xr, double* __restrict__ Xi, int S, int logS, int rows_out, int R,
+                           double scale, const double2* __restrict__ tw) {
+    extern __shared__ double sm[];
+    const Len L{S, logS};
+    const int SP = S + 1;
+    double* re = sm;
+    double* im = re + (size_t)R * SP;
+    double* tmp = im + (size_t)R * SP;
+    const int f = blockIdx.y;
+    const bool real_mode = (idata == nullptr);
+    const int lat_per_cta = real_mode ? 2 * R : R;
+    const int j0 = blockIdx.x * lat_per_cta;
+    const int nlat = min(lat_per_cta, S - j0);
+    const int nseq = real_mode ? (nlat + 1) / 2 : nlat;
+    const size_t gbase = (size_t)f * S * S;
+
+    for (int t = threadIdx.x; t < nseq * S; t += blockDim.x) {
+        const int r = t / S, k = t - r * S;
+        double a, b;
+        if (real_mode) {
+            const int la = j0 + 2 * r, lb = la + 1;
+            a = rdata[gbase + (size_t)la * S + k];
+            b = (lb < j0 + nlat) ? rdata[gbase + (size_t)lb * S + k] : 0.0;
+        } else {
+            a = rdata[gbase + (size_t)(j0 + r) * S + k];
+            b = idata[gbase + (size_t)(j0 + r) * S + k];
+        }
+        re[r * SP + L.pos(k)] = a;
+        im[r * SP + L.pos(k)] = b;
+    }
+    __syncthreads();
+    block_dft<double, double2>(re, im, L, nseq, SP, tw, -1.0, tmp);
+
+    const size_t xbase = (size_t)f * rows_out * S;
+    for (int t = threadIdx.x; t < rows_out * nlat; t += blockDim.x) {
+        const int m = t / nlat, q = t - m * nlat;
+        double vr, vi;
+        if (real_mode) {
+            const int r = q >> 1;
+            const double zr = re[r * SP + m], zi = im[r * SP + m];
+            const int mm = (m == 0) ? 0 : S - m;
+            const double wr = re[r * SP + mm], wi = im[r * SP + mm];
+            if ((q & 1) == 0) {
+                vr = 0.5 * (zr + wr);
+                vi = 0.5 * (zi - wi);
+            } else {
+                vr = 0.5 * (zi + wi);
+                vi = -0.5 * (zr - wr);
+            }
+        } else {
+            vr = re[q * SP + m];
+            vi = im[q * SP + m];
+        }
+        Xr[xbase + (size_t)m * S + j0 + q] = vr * scale;
+        Xi[xbase + (size_t)m * S + j0 + q] = vi * scale;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+struct FwdDlt {
+    const double* Xr;
+    const double* Xi;      // may be null (imaginary input zero)
+    int xrows;             // rows per function in X
+    double* rc;
+    double* ic;            // may be null (imaginary output not wanted)
+    int64_t c_stride;      // doubles between functions in rc/ic
+    const double* tab;
+    const int64_t* off;    // null: `tab` is the table of order m1d
+    const double* w;
+    const double2* twS;
+    const double2* twD;
+    int B, S, logS, cutoff, nfunc, G;
+    int complex_rows;      // rows 0..B-1 and B+1..S-1 (COMPLEX) else 0..B-1
+    int real_mirror;       // fill f(l,-m) = (-1)^m conj f(l,m)
+    int one_d, m1d;        // single order from row 0 of X, output contiguous result[l-m]
+};
+
+__global__ void k_fwd_dlt(FwdDlt p) {
+    extern __shared__ double sm[];
+    const int B = p.B, S = p.S;
+    const Len L{S, p.logS};
+    const int Ge = (p.G + 1) & ~1;
+    int row, m;
+    bool neg = false;
+    if (p.one_d) {
+        row = 0;
+        m = p.m1d;
+    } else {
+        row = blockIdx.x;
+        if (p.complex_rows && row >= B) row += 1;
+        neg = row > B;
+        m = neg ? S - row : row;
+    }
+    const bool semi = m < p.cutoff;
+    const double sgn = (neg && (row & 1)) ? -1.0 : 1.0;
+    const int f0 = blockIdx.y * p.G;
+
+    double* zr = sm;
+    double* zi = zr + S;
+    double* tmp = zi + S;
+    double* cbuf = tmp + (L.pow2() ? 0 : 2 * S);
+    const int clen = semi ? B : S;  // per function per part
+    double* cre = cbuf;                          // [Ge][clen]
+    double* cim = cbuf + (size_t)Ge * clen;      // [Ge][clen]
+    const double* w = p.w + ((semi && (m & 1)) ? S : 0);
+    const int xrow = p.one_d ? 0 : row;
+
+    for (int g = 0; g < Ge; ++g) {
+        const int f = f0 + g;
+        const bool live = (g < p.G) && (f < p.nfunc);
+        const double* xr = p.Xr + ((size_t)f * p.xrows + xrow) * S;
+        const double* xi = p.Xi ? p.Xi + ((size_t)f * p.xrows + xrow) * S : nullptr;
+        if (!semi) {
+            for (int q = threadIdx.x; q < S; q += blockDim.x) {
+                cre[(size_t)g * S + q] = live ? xr[q] * w[q] : 0.0;
+                cim[(size_t)g * S + q] = (live && xi) ? xi[q] * w[q] : 0.0;
+            }
+            continue;
+        }
+        if (!live) {
+            for (int k = threadIdx.x; k < B; k += blockDim.x) {
+                cre[(size_t)g * B + k] = 0.0;
+                cim[(size_t)g * B + k] = 0.0;
+            }
+            continue;
+        }
+        // weighted data, Makhoul reorder (v[j] = x[2j], v[S-1-j] = x[2j+1]) into bit-reversed slots
+        for (int q = threadIdx.x; q < S; q += blockDim.x) {
+            const int d = (q & 1) ? S - 1 - (q >> 1) : (q >> 1);
+            zr[L.pos(d)] = xr[q] * w[q];
+            zi[L.pos(d)] = xi ? xi[q] * w[q] : 0.0;
+        }
+        __syncthreads();
+        block_dft<double, double2>(zr, zi, L, 1, S, p.twS, -1.0, tmp);
+        // REDFT10 of both parts, c[0] *= sqrt(1/2), c *= 1/sqrt(2S)   (seminaive.c:170-176)
+        const double nrm = 1.0 / sqrt(2.0 * S);
+        for (int k = threadIdx.x; k < B; k += blockDim.x) {
+            const int kk = (k == 0) ? 0 : S - k;
+            const double ar = zr[k], ai = zi[k], br = zr[kk], bi = zi[kk];
+            const double c = p.twD[k].x, s = p.twD[k].y;
+            double va = (ar + br) * c + (ai - bi) * s;
+            double vb = (ai + bi) * c - (ar - br) * s;
+            const double f = (k == 0) ? kSqrtHalf * nrm : nrm;
+            cre[(size_t)g * B + k] = va * f;
+            cim[(size_t)g * B + k] = vb * f;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+
+    const int nrows = B - m;
+    const int nch = Ge / 2;
+    const int64_t tab0 = p.off ? p.off[m] : 0;
+    const double* tab = p.tab + tab0;
+    for (int task = threadIdx.x; task < nrows * nch; task += blockDim.x) {
+        const int li = task % nrows, ch = task / nrows;
+        const int l = m + li;
+        const int g0 = 2 * ch, g1 = g0 + 1;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        if (semi) {
+            const int t = li & 1;
+            const int rs = row_size(m, l);
+            const double* trow = tab + table_offset(m, l);
+            const double* c0 = cre + (size_t)g0 * B + t;
+            const double* c1 = cim + (size_t)g0 * B + t;
+            const double* c2 = cre + (size_t)g1 * B + t;
+            const double* c3 = cim + (size_t)g1 * B + t;
+            for (int j = 0; j < rs; ++j) {
+                const double v = trow[j];
+                a0 = fma(v, c0[2 * j], a0);
+                a1 = fma(v, c1[2 * j], a1);
+                a2 = fma(v, c2[2 * j], a2);
+                a3 = fma(v, c3[2 * j], a3);
+            }
+        } else {
+            const double* prow = tab + (size_t)li * S;
+            const double* c0 = cre + (size_t)g0 * S;
+            const double* c1 = cim + (size_t)g0 * S;
+            const double* c2 = cre + (size_t)g1 * S;
+            const double* c3 = cim + (size_t)g1 * S;
+            for (int j = 0; j < S; ++j) {
+                const double v = prow[j];
+                a0 = fma(c0[j], v, a0);
+                a1 = fma(c1[j], v, a1);
+                a2 = fma(c2[j], v, a2);
+                a3 = fma(c3[j], v, a3);
+            }
+        }
+        for (int h = 0; h < 2; ++h) {
+            const int g = g0 + h;
+            const int f = f0 + g;
+            if (g >= p.G || f >= p.nfunc) continue;
+            const double vr = sgn * (h ? a2 : a0), vi = sgn * (h ? a3 : a1);
+            double* rc = p.rc + (size_t)f * p.c_stride;
+            double* ic = p.ic ? p.ic + (size_t)f * p.c_stride : nullptr;
+            const int idx = p.one_d ? li : index_of_harmonic_coeff(neg ? -m : m, l, B);
+            rc[idx] = vr;
+            if (ic) ic[idx] = vi;
+            if (p.real_mirror && m > 0) {
+                const int i2 = index_of_harmonic_coeff(-m, l, B);
+                const double s = (m & 1) ? -1.0 : 1.0;
+                rc[i2] = s * vr;
+                if (ic) ic[i2] = -s * vi;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+struct InvDlt {
+    const double* rc;
+    const double* ic;      // may be null (zero)
+    int64_t c_stride;
+    double* Fr;
+    double* Fi;
+    int frows;
+    const double* tab;     // transposed cosine tables / sampled Pml
+    const int64_t* off;    // null: `tab` is the table of order m1d
+    const double* sinv;
+    const double2* twS;
+    const double2* twD;
+    int B, S, logS, cutoff, nfunc, G;
+    int complex_rows;
+    int one_d, m1d;
+    double out_scale;
+};
+
+__global__ void k_inv_dlt(InvDlt p) {
+    extern __shared__ double sm[];
+    const int B = p.B, S = p.S;
+    const Len L{S, p.logS};
+    const int Ge = (p.G + 1) & ~1;
+    int row, m;
+    bool neg = false;
+    if (p.one_d) {
+        row = 0;
+        m = p.m1d;
+    } else {
+        row = blockIdx.x;
+        if (p.complex_rows && row >= B) row += 1;
+        neg = row > B;
+        m = neg ? S - row : row;
+    }
+    const bool semi = m < p.cutoff;
+    const double sgn = ((neg && (row & 1)) ? -1.0 : 1.0) * p.out_scale;
+    const int f0 = blockIdx.y * p.G;
+    const int nl = B - m;
+
+    double* zr = sm;
+    double* zi = zr + S;
+    double* tmp = zi + S;
+    double* are = tmp + (L.pow2() ? 0 : 2 * S);  // [Ge][B]
+    double* aim = are + (size_t)Ge * B;           // [Ge][B]
+    double* fre = aim + (size_t)Ge * B;           // [Ge][B]  (semi only)
+    double* fim = fre + (size_t)Ge * B;
+    int* toff = (int*)(fim + (size_t)Ge * B);     // B + 1 ints
+    int* wtot = toff + B + 1;                     // 32 ints
+
+    for (int t = threadIdx.x; t < Ge * nl; t += blockDim.x) {
+        const int g = t / nl, li = t - g * nl;
+        const int f = f0 + g;
+        double vr = 0.0, vi = 0.0;
+        if (g < p.G && f < p.nfunc) {
+            const int idx = p.one_d ? li : index_of_harmonic_coeff(neg ? -m : m, m + li, B);
+            vr = p.rc[(size_t)f * p.c_stride + idx];
+            vi = p.ic ? p.ic[(size_t)f * p.c_stride + idx] : 0.0;
+        }
+        are[(size_t)g * B + li] = vr;
+        aim[(size_t)g * B + li] = vi;
+    }
+    const int64_t tab0 = p.off ? p.off[m] : 0;
+    const double* tab = p.tab + tab0;
+    const int nch = Ge / 2;
+
+    if (!semi) {
+        __syncthreads();
+        // naive synthesis: F[q] = sum_l a[l-m] P(m,l)(x_q)
+        for (int task = threadIdx.x; task < S * nch; task += blockDim.x) {
+            const int q = task % S, ch = task / S;
+            const int g0 = 2 * ch;
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            for (int li = 0; li < nl; ++li) {
+                const double v = tab[(size_t)li * S + q];
+                a0 = fma(are[(size_t)g0 * B + li], v, a0);
+                a1 = fma(aim[(size_t)g0 * B + li], v, a1);
+                a2 = fma(are[(size_t)(g0 + 1) * B + li], v, a2);
+                a3 = fma(aim[(size_t)(g0 + 1) * B + li], v, a3);
+            }
+            for (int h = 0; h < 2; ++h) {
+                const int f = f0 + g0 + h;
+                if (g0 + h >= p.G || f >= p.nfunc) continue;
+                const size_t o = ((size_t)f * p.frows + (p.one_d ? 0 : row)) * S + q;
+                p.Fr[o] = sgn * (h ? a2 : a0);
+                if (p.Fi) p.Fi[o] = sgn * (h ? a3 : a1);
+            }
+        }
+        return;
+    }
+
+    // transposed-table row offsets: exclusive scan of Transpose_RowSize(i, m, B)
+    for (int i = threadIdx.x; i < B; i += blockDim.x) toff[i] = transpose_row_size(i, m, B);
+    __syncthreads();
+    block_exclusive_scan(toff, B, wtot);
+
+    const double scale = 0.5 / sqrt((double)B);
+    const double scale0 = 1.0 / sqrt((double)S);
+    for (int task = threadIdx.x; task < B * nch; task += blockDim.x) {
+        const int i = task % B, ch = task / B;
+        const int g0 = 2 * ch;
+        const int rs = transpose_row_size(i, m, B);
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        if (rs > 0) {
+            const int base = trans_first_l(i, m) - m;
+            const double* trow = tab + toff[i];
+            const double* c0 = are + (size_t)g0 * B + base;
+            const double* c1 = aim + (size_t)g0 * B + base;
+            const double* c2 = are + (size_t)(g0 + 1) * B + base;
+            const double* c3 = aim + (size_t)(g0 + 1) * B + base;
+            for (int j = 0; j < rs; ++j) {
+                const double v = trow[j];
+                a0 = fma(c0[2 * j], v, a0);
+                a1 = fma(c1[2 * j], v, a1);
+                a2 = fma(c2[2 * j], v, a2);
+                a3 = fma(c3[2 * j], v, a3);
+            }
+        }
+        const double s = (i == 0) ? scale0 : scale;
+        fre[(size_t)g0 * B + i] = a0 * s;
+        fim[(size_t)g0 * B + i] = a1 * s;
+        fre[(size_t)(g0 + 1) * B + i] = a2 * s;
+        fim[(size_t)(g0 + 1) * B + i] = a3 * s;
+    }
+    __syncthreads();
+
+    // REDFT01 of (fre + i fim) per function, zero-padded from B to S   (seminaive.c:107)
+    for (int g = 0; g < Ge; ++g) {
+        const int f = f0 + g;
+        if (g >= p.G || f >= p.nfunc) break;
+        const double* xa = fre + (size_t)g * B;
+        const double* xb = fim + (size_t)g * B;
+        for (int k = threadIdx.x; k < S; k += blockDim.x) {
+            const double ak = (k < B) ? xa[k] : 0.0, bk = (k < B) ? xb[k] : 0.0;
+            const int r = S - k;  // X[S] = 0
+            const double ar = (k > 0 && r < B) ? xa[r] : 0.0, br = (k > 0 && r < B) ? xb[r] : 0.0;
+            const double wr = ak + br, wi = bk - ar;
+            const double c = p.twD[k].x, s = p.twD[k].y;
+            zr[L.pos(k)] = wr * c - wi * s;
+            zi[L.pos(k)] = wr * s + wi * c;
+        }
+        __syncthreads();
+        block_dft<double, double2>(zr, zi, L, 1, S, p.twS, 1.0, tmp);
+        const size_t ob = ((size_t)f * p.frows + (p.one_d ? 0 : row)) * S;
+        for (int q = threadIdx.x; q < S; q += blockDim.x) {
+            const int src = (q & 1) ? S - 1 - (q >> 1) : (q >> 1);
+            double vr = zr[src], vi = zi[src];
+            if (m & 1) {
+                vr *= p.sinv[q];
+                vi *= p.sinv[q];
+            }
+            p.Fr[ob + q] = sgn * vr;
+            if (p.Fi) p.Fi[ob + q] = sgn * vi;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Inverse DFT along m for each latitude (sign +1), R sequences per CTA.
+//   fmt_complex : rows 0..S-1 from F (row B = 0)
+//   REAL        : rows m > B are conj(F[S-m])
+//   real output (rdata only, idata == null): two latitudes per complex DFT
+__global__ void k_rows_inv(const double* __restrict__ Fr, const double* __restrict__ Fi, int frows, int fmt_complex,
+                           double* __restrict__ rdata, double* __restrict__ idata, int S, int logS, int R,
+                           const double2* __restrict__ tw) {
+    extern __shared__ double sm[];
+    const Len L{S, logS};
+    const int B = S / 2;
+    const int SP = S + 1;
+    double* re = sm;
+    double* im = re + (size_t)R * SP;
+    double* tmp = im + (size_t)R * SP;
+    const int f = blockIdx.y;
+    const bool real_out = (idata == nullptr);
+    const int lat_per_cta = real_out ? 2 * R : R;
+    const int j0 = blockIdx.x * lat_per_cta;
+    const int nlat = min(lat_per_cta, S - j0);
+    const int nseq = real_out ? (nlat + 1) / 2 : nlat;
+    const size_t fb = (size_t)f * frows * S;
+
+    // gather: consecutive threads take consecutive latitudes of one row (coalesced reads)
+    for (int t = threadIdx.x; t < S * nlat; t += blockDim.x) {
+        const int mrow = t / nlat, q = t - mrow * nlat;
+        const int lat = j0 + q;
+        double vr = 0.0, vi = 0.0;
+        if (mrow != B) {
+            if (fmt_complex) {
+                vr = Fr[fb + (size_t)mrow * S + lat];
+                vi = Fi[fb + (size_t)mrow * S + lat];
+            } else if (mrow < B) {
+                vr = Fr[fb + (size_t)mrow * S + lat];
+                vi = Fi[fb + (size_t)mrow * S + lat];
+            } else {
+                vr = Fr[fb + (size_t)(S - mrow) * S + lat];
+                vi = -Fi[fb + (size_t)(S - mrow) * S + lat];
+            }
+        }
+        if (real_out) {
+            if (mrow == 0) vi = 0.0;  // Hermitian: the m = 0 term is real
+            const int r = q >> 1;
+            // Z = F_a + i F_b
+            if ((q & 1) == 0) {
+                re[r * SP + L.pos(mrow)] = vr;
+                im[r * SP + L.pos(mrow)] = vi;
+            }
+            __syncwarp();
+        } else {
+            re[q * SP + L.pos(mrow)] = vr;
+            im[q * SP + L.pos(mrow)] = vi;
+        }
+    }
+    if (real_out) {
+        // second pass: add i * F_b for the odd latitudes (avoids a write race on the same slot)
+        __syncthreads();
+        for (int t = threadIdx.x; t < S * nlat; t += blockDim.x) {
+            const int mrow = t / nlat, q = t - mrow * nlat;
+            if ((q & 1) == 0) continue;
+            const int lat = j0 + q;
+            double vr = 0.0, vi = 0.0;
+            if (mrow != B) {
+                if (mrow < B) {
+                    vr = Fr[fb + (size_t)mrow * S + lat];
+                    vi = Fi[fb + (size_t)mrow * S + lat];
+                } else {
+                    vr = Fr[fb + (size_t)(S - mrow) * S + lat];
+                    vi = -Fi[fb + (size_t)(S - mrow) * S + lat];
+                }
+            }
+            if (mrow == 0) vi = 0.0;
+            const int r = q >> 1;
+            re[r * SP + L.pos(mrow)] -= vi;
+            im[r * SP + L.pos(mrow)] += vr;
+        }
+    }
+    __syncthreads();
+    block_dft<double, double2>(re, im, L, nseq, SP, tw, 1.0, tmp);
+    const size_t gb = (size_t)f * S * S;
+    for (int t = threadIdx.x; t < nlat * S; t += blockDim.x) {
+        const int q = t / S, k = t - q * S;
+        if (real_out) {
+            const int r = q >> 1;
+            rdata[gb + (size_t)(j0 + q) * S + k] = (q & 1) ? im[r * SP + k] : re[r * SP + k];
+        } else {
+            rdata[gb + (size_t)(j0 + q) * S + k] = re[q * SP + k];
+            idata[gb + (size_t)(j0 + q) * S + k] = im[q * SP + k];
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// FZT row sums (FST_semi_memo.c:386-398): X0[f][theta] = sqrt(2 pi)/S * sum_phi data
+__global__ void k_rowsum(const double* __restrict__ rdata, const double* __restrict__ idata, double* Xr, double* Xi,
+                         int S, double scale) {
+    const int f = blockIdx.y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (row >= S) return;
+    const size_t b = (size_t)f * S * S + (size_t)row * S;
+    double sr = 0.0, si = 0.0;
+    for (int k = lane; k < S; k += 32) {
+        sr += rdata[b + k];
+        if (idata) si += idata[b + k];
+    }
+    for (int o = 16; o; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) {
+        Xr[(size_t)f * S + row] = sr * scale;
+        Xi[(size_t)f * S + row] = si * scale;
+    }
+}
+
+// TransMult (util.c:68-103): out = (filter (x) data) * sqrt(4 pi / (2l+1)), with the
+// reference's ComplexMult imaginary part x*v - y*u (util.c:23-27).
+__global__ void k_transmult(const double* __restrict__ rd, const double* __restrict__ id,
+                            const double* __restrict__ rf, const double* __restrict__ iff, double* rr, double* ir,
+                            int B) {
+    const int f = blockIdx.y;
+    const int m = (int)blockIdx.x - (B - 1);
+    const int am = m < 0 ? -m : m;
+    const size_t cb = (size_t)f * B * B;
+    for (int l = am + threadIdx.x; l < B; l += blockDim.x) {
+        const int idx = index_of_harmonic_coeff(m, l, B);
+        const double x = rf[(size_t)f * B + l], y = iff[(size_t)f * B + l];
+        const double u = rd[cb + idx], v = id[cb + idx];
+        const double s = sqrt(4.0 * kPi / (2.0 * l + 1.0));
+        rr[cb + idx] = (x * u - y * v) * s;
+        ir[cb + idx] = (x * v - y * u) * s;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Host-side launchers.
+
+static int rows_per_cta(int S) {
+    int R = 4096 / S;
+    if (R < 1) R = 1;
+    if (R > 32) R = 32;
+    return R;
+}
+
+static size_t rows_smem(int S, int R) {
+    const Len L = make_len(S);
+    return ((size_t)2 * R * (S + 1) + (L.pow2() ? 0 : 2 * S)) * sizeof(double);
+}
+
+static int launch_rows_fwd(const double* rdata, const double* idata, double* Xr, double* Xi, int B, int rows_out,
+                           int batch, const double2* tw, cudaStream_t st) {
+    const int S = 2 * B;
+    const Len L = make_len(S);
+    const int R = rows_per_cta(S);
+    const int lat_per = idata ? R : 2 * R;
+    const size_t smem = rows_smem(S, R);
+    S2G_TRY(set_smem((const void*)k_rows_fwd, smem));
+    dim3 grid((S + lat_per - 1) / lat_per, batch);
+    k_rows_fwd<<<grid, 256, smem, st>>>(rdata, idata, Xr, Xi, S, L.logn, rows_out, R, sqrt(2.0 * kPi) / S, tw);
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+static int pick_group(int B, int S, bool naive, bool pow2, size_t* smem_out, size_t per_g_extra = 0) {
+    const size_t fixed = ((size_t)2 * S + (pow2 ? 0 : 2 * S)) * sizeof(double);
+    const size_t per_g = (size_t)2 * (naive ? S : B) * sizeof(double) + per_g_extra;
+    const size_t budget = 160 * 1024;
+    int G = 8;
+    while (G > 2 && fixed + (size_t)G * per_g > budget) G -= 2;
+    if (fixed + (size_t)G * per_g > 220 * 1024) return 0;
+    *smem_out = fixed + (size_t)G * per_g;
+    return G;
+}
+
+static int launch_fwd_dlt(FwdDlt p, int nrows_grid, cudaStream_t st) {
+    const Len L = make_len(p.S);
+    size_t smem = 0;
+    const bool any_naive = p.one_d ? (p.m1d >= p.cutoff) : (p.cutoff < p.B);
+    const int G = pick_group(p.B, p.S, any_naive, L.pow2(), &smem);
+    if (!G) return fail(S2G_ERR_UNSUPPORTED, "bandwidth %d too large for the FP64 DLT kernel", p.B);
+    p.G = G;
+    p.logS = L.logn;
+    S2G_TRY(set_smem((const void*)k_fwd_dlt, smem));
+    dim3 grid(nrows_grid, (p.nfunc + G - 1) / G);
+    k_fwd_dlt<<<grid, 256, smem, st>>>(p);
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+static int launch_inv_dlt(InvDlt p, int nrows_grid, cudaStream_t st) {
+    const Len L = make_len(p.S);
+    // are, aim, fre, fim: 4*B per function; plus B+33 ints
+    const size_t fixed = ((size_t)2 * p.S + (L.pow2() ? 0 : 2 * p.S)) * sizeof(double) +
+                         (size_t)(p.B + 1 + 32) * sizeof(int);
+    const size_t per_g = (size_t)4 * p.B * sizeof(double);
+    int G = 8;
+    while (G > 2 && fixed + (size_t)G * per_g > 160 * 1024) G -= 2;
+    const size_t smem = fixed + (size_t)G * per_g;
+    if (smem > 220 * 1024) return fail(S2G_ERR_UNSUPPORTED, "bandwidth %d too large for the FP64 DLT kernel", p.B);
+    p.G = G;
+    p.logS = L.logn;
+    S2G_TRY(set_smem((const void*)k_inv_dlt, smem));
+    dim3 grid(nrows_grid, (p.nfunc + G - 1) / G);
+    k_inv_dlt<<<grid, 256, smem, st>>>(p);
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+size_t f64_work_bytes(int bw, int batch, int data_format) {
+    const size_t S = 2 * (size_t)bw;
+    const size_t rows = (data_format == COMPLEX) ? S : (size_t)bw;
+    return 2 * (size_t)batch * rows * S * sizeof(double);
+}
+
+int fst_f64(const Tables* t, const double* rdata, const double* idata, double* rc, double* ic, int batch,
+            int data_format, int cutoff, void* work, cudaStream_t st) {
+    const int B = t->bw, S = 2 * B;
+    const int rows = (data_format == COMPLEX) ? S : B;
+    double* Xr = (double*)work;
+    double* Xi = Xr + (size_t)batch * rows * S;
+    // REAL data with no imaginary samples: the packed real path (imaginary part zero)
+    S2G_TRY(launch_rows_fwd(rdata, idata, Xr, Xi, B, rows, batch, t->tw_S, st));
+    FwdDlt p{};
+    p.Xr = Xr;
+    p.Xi = Xi;
+    p.xrows = rows;
+    p.rc = rc;
+    p.ic = ic;
+    p.c_stride = (int64_t)B * B;
+    p.tab = t->fwd;
+    p.off = t->off;
+    p.w = t->weights;
+    p.twS = t->tw_S;
+    p.twD = t->tw_D;
+    p.B = B;
+    p.S = S;
+    p.cutoff = cutoff;
+    p.nfunc = batch;
+    p.complex_rows = (data_format == COMPLEX);
+    p.real_mirror = (data_format != COMPLEX);
+    return launch_fwd_dlt(p, (data_format == COMPLEX) ? S - 1 : B, st);
+}
+
+int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rdata, double* idata, int batch,
+                int data_format, int cutoff, void* work, cudaStream_t st) {
+    const int B = t->bw, S = 2 * B;
+    const int rows = (data_format == COMPLEX) ? S : B;
+    double* Fr = (double*)work;
+    double* Fi = Fr + (size_t)batch * rows * S;
+    InvDlt p{};
+    p.rc = rc;
+    p.ic = ic;
+    p.c_stride = (int64_t)B * B;
+    p.Fr = Fr;
+    p.Fi = Fi;
+    p.frows = rows;
+    p.tab = t->inv;
+    p.off = t->off;
+    p.sinv = t->sinv;
+    p.twS = t->tw_S;
+    p.twD = t->tw_D;
+    p.B = B;
+    p.S = S;
+    p.cutoff = cutoff;
+    p.nfunc = batch;
+    p.complex_rows = (data_format == COMPLEX);
+    p.out_scale = 1.0 / sqrt(2.0 * kPi);  // FST_semi_memo.c:344-348
+    S2G_TRY(launch_inv_dlt(p, (data_format == COMPLEX) ? S - 1 : B, st));
+    const Len L = make_len(S);
+    const int R = rows_per_cta(S);
+    const int lat_per = idata ? R : 2 * R;
+    const size_t smem = rows_smem(S, R);
+    S2G_TRY(set_smem((const void*)k_rows_inv, smem));
+    dim3 grid((S + lat_per - 1) / lat_per, batch);
+    k_rows_inv<<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L.logn, R, t->tw_S);
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+int fzt_f64(const Tables* t, const double* rdata, const double* idata, double* rres, double* ires, int batch,
+            int data_format, void* work, cudaStream_t st) {
+    const int B = t->bw, S = 2 * B;
+    double* Xr = (double*)work;
+    double* Xi = Xr + (size_t)batch * S;
+    dim3 g1((S + 7) / 8, batch);
+    k_rowsum<<<g1, 256, 0, st>>>(rdata, idata, Xr, Xi, S, sqrt(2.0 * kPi) / S);
+    S2G_CUDA(cudaGetLastError());
+    FwdDlt p{};
+    p.Xr = Xr;
+    p.Xi = (data_format == COMPLEX) ? Xi : nullptr;
+    p.xrows = 1;
+    p.rc = rres;
+    p.ic = (data_format == COMPLEX) ? ires : nullptr;
+    p.c_stride = B;
+    p.tab = t->fwd;   // order 0 starts at offset 0 (cutoff >= 1)
+    p.off = nullptr;
+    p.w = t->weights;
+    p.twS = t->tw_S;
+    p.twD = t->tw_D;
+    p.B = B;
+    p.S = S;
+    p.cutoff = B;  // FZT is always seminaive (DLTSemi, FST_semi_memo.c:401)
+    p.nfunc = batch;
+    p.one_d = 1;
+    p.m1d = 0;
+    S2G_TRY(launch_fwd_dlt(p, 1, st));
+    if (data_format != COMPLEX) S2G_CUDA(cudaMemsetAsync(ires, 0, sizeof(double) * (size_t)batch * B, st));
+    return S2G_OK;
+}
+
+int transmult_f64(const double* rd, const double* id, const double* rf, const double* iff, double* rr, double* ir,
+                  int bw, int batch, cudaStream_t st) {
+    dim3 grid(2 * bw - 1, batch);
+    k_transmult<<<grid, 128, 0, st>>>(rd, id, rf, iff, rr, ir, bw);
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+// 1-D transforms (DLTSemi etc.) on device buffers; `table` is the caller's table for order m.
+int dlt_semi_f64(const double* data, int bw, int m, double* result, const double* table, const double* weights,
+                 const double2* twS, const double2* twD, cudaStream_t st) {
+    FwdDlt p{};
+    p.Xr = data;
+    p.xrows = 1;
+    p.rc = result;
+    p.c_stride = bw;
+    p.tab = table;
+    p.w = weights;
+    p.twS = twS;
+    p.twD = twD;
+    p.B = bw;
+    p.S = 2 * bw;
+    p.cutoff = bw;
+    p.nfunc = 1;
+    p.one_d = 1;
+    p.m1d = m;
+    return launch_fwd_dlt(p, 1, st);
+}
+
+int dlt_naive_f64(const double* data, int bw, int m, const double* weights, double* result, const double* ptable,
+                  cudaStream_t st) {
+    FwdDlt p{};
+    p.Xr = data;
+    p.xrows = 1;
+    p.rc = result;
+    p.c_stride = bw;
+    p.tab = ptable;
+    p.w = weights;
+    p.B = bw;
+    p.S = 2 * bw;
+    p.cutoff = 0;  // naive
+    p.nfunc = 1;
+    p.one_d = 1;
+    p.m1d = m;
+    return launch_fwd_dlt(p, 1, st);
+}
+
+int inv_dlt_semi_f64(const double* coeffs, int bw, int m, double* result, const double* ttable, const double* sinv,
+                     const double2* twS, const double2* twD, cudaStream_t st) {
+    InvDlt p{};
+    p.rc = coeffs;
+    p.c_stride = bw;
+    p.Fr = result;
+    p.frows = 1;
+    p.tab = ttable;
+    p.sinv = sinv;
+    p.twS = twS;
+    p.twD = twD;
+    p.B = bw;
+    p.S = 2 * bw;
+    p.cutoff = bw;
+    p.nfunc = 1;
+    p.one_d = 1;
+    p.m1d = m;
+    p.out_scale = 1.0;
+    return launch_inv_dlt(p, 1, st);
+}
+
+int inv_dlt_naive_f64(const double* coeffs, int bw, int m, double* result, const double* ptable, cudaStream_t st) {
+    InvDlt p{};
+    p.rc = coeffs;
+    p.c_stride = bw;
+    p.Fr = result;
+    p.frows = 1;
+    p.tab = ptable;
+    p.B = bw;
+    p.S = 2 * bw;
+    p.cutoff = 0;
+    p.nfunc = 1;
+    p.one_d = 1;
+    p.m1d = m;
+    p.out_scale = 1.0;
+    return launch_inv_dlt(p, 1, st);
+}
+
+}  // namespace s2g

@@ -1,0 +1,130 @@
+"""Generate the committed golden fixtures in tests/golden/ from the S2kit reference.
+
+Run in a container that has the reference checkout (default /root/reference, or
+$S2_REFERENCE_DIR):
+
+    python tests/golden/make_golden.py
+
+Two kinds of fixture are written (all float64, np.savez_compressed):
+
+* copied reference data (data/*.dat of the reference repository), converted to binary:
+  - conv_bw64.npz / conv_bw128.npz : signal, filter and the golden real part of
+    ConvOn2SphereSemiMemo produced by the reference with real FFTW3
+    (data/s64.dat, f64.dat, o64_conv_semi_memo_original.dat and the 128 versions);
+  - ka_<name>.npz : the analytic known-answer sample files y20_bw8, y31_bw8, y43_bw23,
+    yMix_bw17 (interleaved re/im, latitude-major) with the expected coefficients
+    documented for them (Y_2^0, Y_3^1, (sqrt2 + pi i) Y_4^3, Y_1^1 + (3-2i) Y_5^-2).
+* outputs of the unmodified reference C sources compiled by `make -C oracle ref`
+  (FSTSemiMemo, InvFSTSemiMemo, FZTSemiMemo, ConvOn2SphereSemiMemo, DLTSemi/InvDLTSemi,
+  table generators, GenerateWeightsForDLT) on seeded inputs -> ref_*.npz.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle.oracle import COMPLEX, REAL, Reference  # noqa: E402
+
+REF = os.environ.get("S2_REFERENCE_DIR", "/root/reference")
+
+
+def real_field_coeffs(rng, bw, p=0.0):
+    """Complex N(0,1)*(1+l)^-p coefficients with f(l,-m) = (-1)^m conj f(l,m), f(l,0) real."""
+    from oracle.oracle import Oracle
+    o = Oracle()
+    rc = np.zeros(bw * bw)
+    ic = np.zeros(bw * bw)
+    for m in range(bw):
+        for l in range(m, bw):
+            s = (1.0 + l) ** (-p)
+            x, y = rng.standard_normal(2) * s
+            if m == 0:
+                y = 0.0
+            i0 = o.index(m, l, bw)
+            rc[i0], ic[i0] = x, y
+            if m:
+                i1 = o.index(-m, l, bw)
+                rc[i1], ic[i1] = (-1) ** m * x, -((-1) ** m) * y
+    return rc, ic
+
+
+def main():
+    r = Reference()
+    out = HERE
+
+    # ---- copied reference data --------------------------------------------------------
+    for bw in (64, 128):
+        s = np.loadtxt(os.path.join(REF, "data", f"s{bw}.dat"))
+        f = np.loadtxt(os.path.join(REF, "data", f"f{bw}.dat"))
+        o = np.loadtxt(os.path.join(REF, "data", f"o{bw}_conv_semi_memo_original.dat"))
+        np.savez_compressed(os.path.join(out, f"conv_bw{bw}.npz"), signal=s, filter=f, golden=o, bw=bw)
+
+    ka = {
+        "y20_bw8": (8, [(0, 2, 1.0)]),
+        "y31_bw8": (8, [(1, 3, 1.0)]),
+        "y43_bw23": (23, [(3, 4, np.sqrt(2.0) + np.pi * 1j)]),
+        "yMix_bw17": (17, [(1, 1, 1.0), (-2, 5, 3.0 - 2.0j)]),
+    }
+    for name, (bw, terms) in ka.items():
+        d = np.loadtxt(os.path.join(REF, "data", f"{name}.dat")).reshape(-1, 2)
+        exp = np.array([(m, l, complex(v).real, complex(v).imag) for (m, l, v) in terms])
+        np.savez_compressed(os.path.join(out, f"ka_{name}.npz"), rdata=d[:, 0], idata=d[:, 1], bw=bw,
+                            expected=exp)
+
+    # ---- reference outputs on seeded inputs ----------------------------------------
+    rng = np.random.default_rng(20240601)
+    # round trips through the reference API (BASELINE config 1 uses B=64, p=0)
+    cases = [(8, 8, COMPLEX, 0.0), (16, 4, COMPLEX, 0.0), (32, 32, REAL, 1.0), (64, 64, REAL, 0.0),
+             (64, 16, COMPLEX, 1.0)]
+    for bw, cut, fmt, p in cases:
+        if fmt == REAL:
+            rc, ic = real_field_coeffs(rng, bw, p)
+        else:
+            rc = rng.standard_normal(bw * bw)
+            ic = rng.standard_normal(bw * bw)
+        grid_r, grid_i = r.inv_fst(rc, ic, bw, fmt, cut)
+        # forward on an independent (noisy) grid too, so FST is checked off the band-limited subspace
+        nr = rng.standard_normal(4 * bw * bw)
+        ni = rng.standard_normal(4 * bw * bw) if fmt == COMPLEX else np.zeros(4 * bw * bw)
+        frc, fic = r.fst(nr, ni, bw, fmt, cut)
+        brc, bic = r.fst(grid_r, grid_i, bw, fmt, cut)
+        np.savez_compressed(os.path.join(out, f"ref_sht_bw{bw}_cut{cut}_{'real' if fmt else 'complex'}.npz"),
+                            bw=bw, cutoff=cut, fmt=fmt, rcoeffs=rc, icoeffs=ic, inv_r=grid_r, inv_i=grid_i,
+                            noise_r=nr, noise_i=ni, fwd_noise_r=frc, fwd_noise_i=fic, rt_r=brc, rt_i=bic)
+
+    # FZT (REAL and COMPLEX) and TransMult at bw=16
+    bw = 16
+    dr = rng.standard_normal(4 * bw * bw)
+    di = rng.standard_normal(4 * bw * bw)
+    zr, zi = r.fzt(dr, di, bw, COMPLEX)
+    zr2, zi2 = r.fzt(dr, di, bw, REAL)
+    a = rng.standard_normal((4, bw * bw))
+    fr = rng.standard_normal(bw)
+    fi = np.zeros(bw)
+    tr = np.zeros(bw * bw)
+    ti = np.zeros(bw * bw)
+    ptr = lambda x: x.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_double))  # noqa: E731
+    ad, ai = a[0].copy(), a[1].copy()
+    r.lib.TransMult(ptr(ad), ptr(ai), ptr(fr), ptr(fi), ptr(tr), ptr(ti), bw)
+    np.savez_compressed(os.path.join(out, "ref_fzt_transmult_bw16.npz"), bw=bw, data_r=dr, data_i=di,
+                        fzt_complex_r=zr, fzt_complex_i=zi[:bw], fzt_real_r=zr2, fzt_real_i=zi2,
+                        tm_data_r=ad, tm_data_i=ai, tm_filter_r=fr, tm_filter_i=fi, tm_out_r=tr, tm_out_i=ti)
+
+    # tables and weights at bw=16 (cutoff 16 and cutoff 5), weights at 64
+    for bw, cut in ((16, 16), (16, 5)):
+        _, _, fwd, inv = r.tables(bw, cut)
+        np.savez_compressed(os.path.join(out, f"ref_tables_bw{bw}_cut{cut}.npz"), bw=bw, cutoff=cut, fwd=fwd,
+                            inv=inv)
+    np.savez_compressed(os.path.join(out, "ref_weights.npz"), w16=r.weights(16), w64=r.weights(64),
+                        w256=r.weights(256))
+
+    print("fixtures written to", out)
+
+
+if __name__ == "__main__":
+    main()
