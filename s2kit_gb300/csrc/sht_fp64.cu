@@ -17,6 +17,7 @@
 // The real-field fast path (no imaginary samples) packs two latitudes into one complex DFT.
 #include <math.h>
 
+#include "rows.cuh"
 #include "s2g_common.cuh"
 #include "s2g_internal.h"
 
@@ -49,70 +50,6 @@ int twiddles_device(int n, double2* d_full, double2* d_quarter, cudaStream_t st)
 static int set_smem(const void* fn, size_t bytes) {
     if (bytes > 48 * 1024) S2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return S2G_OK;
-}
-
-// ------------------------------------------------------------------------------------
-// Row DFTs along phi.  One CTA: R complex sequences of length S.
-//   complex mode (idata != null): sequence r = latitude j0 + r
-//   real mode    (idata == null): sequence r = latitudes j0 + 2r (real part), j0 + 2r + 1 (imag part)
-// Output X[f][m][theta] for m < rows_out, scaled.
-__global__ void k_rows_fwd(const double* __restrict__ rdata, const double* __restrict__ idata,
-                           double* __restrict__ Xr, double* __restrict__ Xi, int S, int logS, int rows_out, int R,
-                           double scale, const double2* __restrict__ tw) {
-    extern __shared__ double sm[];
-    const Len L{S, logS};
-    const int SP = S + 1;
-    double* re = sm;
-    double* im = re + (size_t)R * SP;
-    double* tmp = im + (size_t)R * SP;
-    const int f = blockIdx.y;
-    const bool real_mode = (idata == nullptr);
-    const int lat_per_cta = real_mode ? 2 * R : R;
-    const int j0 = blockIdx.x * lat_per_cta;
-    const int nlat = min(lat_per_cta, S - j0);
-    const int nseq = real_mode ? (nlat + 1) / 2 : nlat;
-    const size_t gbase = (size_t)f * S * S;
-
-    for (int t = threadIdx.x; t < nseq * S; t += blockDim.x) {
-        const int r = t / S, k = t - r * S;
-        double a, b;
-        if (real_mode) {
-            const int la = j0 + 2 * r, lb = la + 1;
-            a = rdata[gbase + (size_t)la * S + k];
-            b = (lb < j0 + nlat) ? rdata[gbase + (size_t)lb * S + k] : 0.0;
-        } else {
-            a = rdata[gbase + (size_t)(j0 + r) * S + k];
-            b = idata[gbase + (size_t)(j0 + r) * S + k];
-        }
-        re[r * SP + L.pos(k)] = a;
-        im[r * SP + L.pos(k)] = b;
-    }
-    __syncthreads();
-    block_dft<double, double2>(re, im, L, nseq, SP, tw, -1.0, tmp);
-
-    const size_t xbase = (size_t)f * rows_out * S;
-    for (int t = threadIdx.x; t < rows_out * nlat; t += blockDim.x) {
-        const int m = t / nlat, q = t - m * nlat;
-        double vr, vi;
-        if (real_mode) {
-            const int r = q >> 1;
-            const double zr = re[r * SP + m], zi = im[r * SP + m];
-            const int mm = (m == 0) ? 0 : S - m;
-            const double wr = re[r * SP + mm], wi = im[r * SP + mm];
-            if ((q & 1) == 0) {
-                vr = 0.5 * (zr + wr);
-                vi = 0.5 * (zi - wi);
-            } else {
-                vr = 0.5 * (zi + wi);
-                vi = -0.5 * (zr - wr);
-            }
-        } else {
-            vr = re[q * SP + m];
-            vi = im[q * SP + m];
-        }
-        Xr[xbase + (size_t)m * S + j0 + q] = vr * scale;
-        Xi[xbase + (size_t)m * S + j0 + q] = vi * scale;
-    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -424,98 +361,6 @@ __global__ void k_inv_dlt(InvDlt p) {
 }
 
 // ------------------------------------------------------------------------------------
-// Inverse DFT along m for each latitude (sign +1), R sequences per CTA.
-//   fmt_complex : rows 0..S-1 from F (row B = 0)
-//   REAL        : rows m > B are conj(F[S-m])
-//   real output (rdata only, idata == null): two latitudes per complex DFT
-__global__ void k_rows_inv(const double* __restrict__ Fr, const double* __restrict__ Fi, int frows, int fmt_complex,
-                           double* __restrict__ rdata, double* __restrict__ idata, int S, int logS, int R,
-                           const double2* __restrict__ tw) {
-    extern __shared__ double sm[];
-    const Len L{S, logS};
-    const int B = S / 2;
-    const int SP = S + 1;
-    double* re = sm;
-    double* im = re + (size_t)R * SP;
-    double* tmp = im + (size_t)R * SP;
-    const int f = blockIdx.y;
-    const bool real_out = (idata == nullptr);
-    const int lat_per_cta = real_out ? 2 * R : R;
-    const int j0 = blockIdx.x * lat_per_cta;
-    const int nlat = min(lat_per_cta, S - j0);
-    const int nseq = real_out ? (nlat + 1) / 2 : nlat;
-    const size_t fb = (size_t)f * frows * S;
-
-    // gather: consecutive threads take consecutive latitudes of one row (coalesced reads)
-    for (int t = threadIdx.x; t < S * nlat; t += blockDim.x) {
-        const int mrow = t / nlat, q = t - mrow * nlat;
-        const int lat = j0 + q;
-        double vr = 0.0, vi = 0.0;
-        if (mrow != B) {
-            if (fmt_complex) {
-                vr = Fr[fb + (size_t)mrow * S + lat];
-                vi = Fi[fb + (size_t)mrow * S + lat];
-            } else if (mrow < B) {
-                vr = Fr[fb + (size_t)mrow * S + lat];
-                vi = Fi[fb + (size_t)mrow * S + lat];
-            } else {
-                vr = Fr[fb + (size_t)(S - mrow) * S + lat];
-                vi = -Fi[fb + (size_t)(S - mrow) * S + lat];
-            }
-        }
-        if (real_out) {
-            if (mrow == 0) vi = 0.0;  // Hermitian: the m = 0 term is real
-            const int r = q >> 1;
-            // Z = F_a + i F_b
-            if ((q & 1) == 0) {
-                re[r * SP + L.pos(mrow)] = vr;
-                im[r * SP + L.pos(mrow)] = vi;
-            }
-            __syncwarp();
-        } else {
-            re[q * SP + L.pos(mrow)] = vr;
-            im[q * SP + L.pos(mrow)] = vi;
-        }
-    }
-    if (real_out) {
-        // second pass: add i * F_b for the odd latitudes (avoids a write race on the same slot)
-        __syncthreads();
-        for (int t = threadIdx.x; t < S * nlat; t += blockDim.x) {
-            const int mrow = t / nlat, q = t - mrow * nlat;
-            if ((q & 1) == 0) continue;
-            const int lat = j0 + q;
-            double vr = 0.0, vi = 0.0;
-            if (mrow != B) {
-                if (mrow < B) {
-                    vr = Fr[fb + (size_t)mrow * S + lat];
-                    vi = Fi[fb + (size_t)mrow * S + lat];
-                } else {
-                    vr = Fr[fb + (size_t)(S - mrow) * S + lat];
-                    vi = -Fi[fb + (size_t)(S - mrow) * S + lat];
-                }
-            }
-            if (mrow == 0) vi = 0.0;
-            const int r = q >> 1;
-            re[r * SP + L.pos(mrow)] -= vi;
-            im[r * SP + L.pos(mrow)] += vr;
-        }
-    }
-    __syncthreads();
-    block_dft<double, double2>(re, im, L, nseq, SP, tw, 1.0, tmp);
-    const size_t gb = (size_t)f * S * S;
-    for (int t = threadIdx.x; t < nlat * S; t += blockDim.x) {
-        const int q = t / S, k = t - q * S;
-        if (real_out) {
-            const int r = q >> 1;
-            rdata[gb + (size_t)(j0 + q) * S + k] = (q & 1) ? im[r * SP + k] : re[r * SP + k];
-        } else {
-            rdata[gb + (size_t)(j0 + q) * S + k] = re[q * SP + k];
-            idata[gb + (size_t)(j0 + q) * S + k] = im[q * SP + k];
-        }
-    }
-}
-
-// ------------------------------------------------------------------------------------
 // FZT row sums (FST_semi_memo.c:386-398): X0[f][theta] = sqrt(2 pi)/S * sum_phi data
 __global__ void k_rowsum(const double* __restrict__ rdata, const double* __restrict__ idata, double* Xr, double* Xi,
                          int S, double scale) {
@@ -580,9 +425,9 @@ static int launch_rows_fwd(const double* rdata, const double* idata, double* Xr,
     const int R = rows_per_cta(S);
     const int lat_per = idata ? R : 2 * R;
     const size_t smem = rows_smem(S, R);
-    S2G_TRY(set_smem((const void*)k_rows_fwd, smem));
+    S2G_TRY(set_smem((const void*)k_rows_fwd<double, double2>, smem));
     dim3 grid((S + lat_per - 1) / lat_per, batch);
-    k_rows_fwd<<<grid, 256, smem, st>>>(rdata, idata, Xr, Xi, S, L.logn, rows_out, R, sqrt(2.0 * kPi) / S, tw);
+    k_rows_fwd<double, double2><<<grid, 256, smem, st>>>(rdata, idata, Xr, Xi, S, L.logn, rows_out, R, sqrt(2.0 * kPi) / S, tw);
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -696,9 +541,9 @@ int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rda
     const int R = rows_per_cta(S);
     const int lat_per = idata ? R : 2 * R;
     const size_t smem = rows_smem(S, R);
-    S2G_TRY(set_smem((const void*)k_rows_inv, smem));
+    S2G_TRY(set_smem((const void*)k_rows_inv<double, double2>, smem));
     dim3 grid((S + lat_per - 1) / lat_per, batch);
-    k_rows_inv<<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L.logn, R, t->tw_S);
+    k_rows_inv<double, double2><<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L.logn, R, t->tw_S);
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }

@@ -50,8 +50,9 @@ def _inv(rc, ic, bw, fmt, cutoff, tt=None):
 def test_tables_match_reference(golden, bw, cut):
     g = golden(f"ref_tables_bw{bw}_cut{cut}")
     t, tt = _tables(bw, cut)
-    assert np.abs(t.space - g["fwd"]).max() <= 1e-14
-    assert np.abs(tt.space - g["inv"]).max() <= 1e-14
+    scale = np.abs(g["fwd"]).max()
+    assert np.abs(t.space - g["fwd"]).max() <= 1e-13 * scale
+    assert np.abs(tt.space - g["inv"]).max() <= 1e-13 * scale
 
 
 @pytest.mark.parametrize("bw", [64, 256, 512])
@@ -89,13 +90,15 @@ def test_single_order_builders(oracle):
         n = api.TableSize(m, bw)
         tab = np.zeros(n)
         api.GenerateCosPmlTable(bw, m, tab, None)
-        assert np.abs(tab - oracle.cos_pml_table(bw, m)).max() <= 1e-14
+        ref = oracle.cos_pml_table(bw, m)
+        assert np.abs(tab - ref).max() <= 1e-13 * np.abs(ref).max()
         tr = np.zeros(n)
         api.TransposeCosPmlTable(bw, m, tab, tr)
         assert np.abs(tr - oracle.transpose_cos_pml_table(bw, m, tab)).max() == 0.0
         p = np.zeros(2 * bw * (bw - m))
         api.GeneratePmlTable(bw, m, p, None)
-        assert np.abs(p - oracle.pml_table(bw, m)).max() <= 1e-13
+        ref = oracle.pml_table(bw, m)
+        assert np.abs(p - ref).max() <= 1e-13 * np.abs(ref).max()
 
 
 # ------------------------------------------------------------------------- known answers
