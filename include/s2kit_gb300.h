@@ -138,7 +138,7 @@ int s2g_cache_clear(void);
 
 typedef struct s2g_plan_s* s2g_plan;
 
-/* Creates a plan for bandwidth bw (even, 2 <= bw <= 4096 for FP64; odd bw up to 255) and a
+/* Creates a plan for bandwidth bw (2 <= bw <= 2048 for powers of two, any bw <= 512 otherwise) and a
  * seminaive/naive cutoff (1 <= cutoff <= bw).  Tables are generated on the current device
  * (FP64 recurrence and DCT, cospml.c:161-242) and shared by every plan with the same
  * (device, bw, cutoff). */
@@ -157,20 +157,21 @@ int s2g_fst(s2g_plan plan, const double* rdata, const double* idata, double* rco
             DataFormat data_format, void* stream);
 int s2g_inv_fst(s2g_plan plan, const double* rcoeffs, const double* icoeffs, double* rdata, double* idata,
                 int batch, DataFormat data_format, void* stream);
-/* Zonal transform of `batch` functions: rres/ires hold bw (COMPLEX) values per function;
- * REAL zeroes 2*bw imaginary values per function as the reference does. */
+/* Zonal transform of `batch` functions: rres/ires hold bw values per function (REAL
+ * zeroes the imaginary part; the host drop-in FZTSemiMemo zeroes 2*bw as the reference). */
 int s2g_fzt(s2g_plan plan, const double* rdata, const double* idata, double* rres, double* ires, int batch,
             DataFormat data_format, void* stream);
 /* Coefficient-space product with a zonal filter (TransMult), batched. */
 int s2g_transmult(int bw, const double* rdatacoeffs, const double* idatacoeffs, const double* rfiltercoeffs,
                   const double* ifiltercoeffs, double* rres, double* ires, int batch, void* stream);
-/* Convolution of `batch` real functions with one zonal filter (ConvOn2SphereSemiMemo),
- * plan must have cutoff == bw. */
+/* Convolution of `batch` pairs (data_f, filter_f), each as ConvOn2SphereSemiMemo, both
+ * grids batch*(2bw)^2; the plan must have cutoff == bw. */
 int s2g_conv(s2g_plan plan, const double* rdata, const double* idata, const double* rfilter,
              const double* ifilter, double* rres, double* ires, int batch, void* stream);
 
 /* Real-field batched transforms with FP32 samples/coefficients and a selectable
- * precision for the Legendre contraction (s2g_precision).  grid: batch*(2bw)^2 floats;
+ * precision for the Legendre contraction (s2g_precision); power-of-two bw in [16, 512],
+ * plan cutoff == bw.  grid: batch*(2bw)^2 floats;
  * rcoeffs/icoeffs: batch*bw*bw floats in the reference layout, negative orders filled by
  * f(l,-m) = (-1)^m conj f(l,m) on output and ignored on input. */
 int s2g_fst_real_f32(s2g_plan plan, const float* grid, float* rcoeffs, float* icoeffs, int batch, int precision,
@@ -184,6 +185,17 @@ int s2g_fst_real_f32_host(s2g_plan plan, const float* grid, float* rcoeffs, floa
                           int precision);
 int s2g_inv_fst_real_f32_host(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid, int batch,
                               int precision);
+
+/* Waits for the plan's device work and reports a failure recorded on the device by the
+ * tensor-core kernels (S2G_ERR_TIMEOUT when a bounded wait expired); clears the record. */
+int s2g_plan_sync_status(s2g_plan plan);
+
+/* ========================== Part 3: diagnostics =================================== */
+
+/* Runs the split-BF16 tcgen05 machinery on one tile: D[128 x N] = A[128 x K] * B[N x K]^T
+ * (row-major FP32 device arrays, N and K multiples of 16, N <= 256, K <= 128) with `nprod`
+ * of the six split products (1 = plain BF16 ... 6 = 3-term split).  Synchronous. */
+int s2g_selftest_tc(int N, int K, int nprod, const float* A, const float* B, float* D);
 
 #ifdef __cplusplus
 }

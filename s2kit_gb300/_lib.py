@@ -62,6 +62,8 @@ SIGNATURES = {
     "s2g_inv_fst_real_f32": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, vp]),
     "s2g_fst_real_f32_host": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
     "s2g_inv_fst_real_f32_host": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
+    "s2g_plan_sync_status": (C.c_int, [vp]),
+    "s2g_selftest_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, vp]),
 }
 
 _lib = None

@@ -187,6 +187,10 @@ class Plan:
         except Exception:
             pass
 
+    def sync_status(self):
+        """Waits for the device and raises if a tensor-core kernel recorded a failure."""
+        check(self.lib.s2g_plan_sync_status(self.h), "device status")
+
     def workspace_size(self, batch: int, precision: int = PREC_FP64) -> int:
         return self.lib.s2g_plan_workspace_size(self.h, batch, precision)
 
@@ -221,6 +225,11 @@ class Plan:
     def inv_fst_real_f32_host(self, rcoeffs: np.ndarray, icoeffs: np.ndarray, grid: np.ndarray, batch, precision):
         check(self.lib.s2g_inv_fst_real_f32_host(self.h, rcoeffs.ctypes.data, icoeffs.ctypes.data, grid.ctypes.data,
                                                  batch, precision), "s2g_inv_fst_real_f32_host")
+
+
+def selftest_tc(A, B, D, nprod=6):
+    """D = A @ B.T on one tcgen05 tile (torch CUDA float32 tensors, A 128 x K, B N x K)."""
+    check(load().s2g_selftest_tc(B.shape[0], A.shape[1], nprod, _addr(A), _addr(B), _addr(D)), "s2g_selftest_tc")
 
 
 def transmult(bw, rd, id_, rf, if_, rr, ir, batch, stream=None):

@@ -776,6 +776,13 @@ int s2g_inv_fst_real_f32(s2g_plan p, const float* rc, const float* ic, float* gr
     return inv_fst_split(p->t, rc, ic, grid, batch, precision, p->work.ptr, (cudaStream_t)stream);
 }
 
+int s2g_plan_sync_status(s2g_plan p) {
+    if (!p) return fail(S2G_ERR_ARG, "NULL plan");
+    S2G_CUDA(cudaSetDevice(p->device));
+    S2G_CUDA(cudaDeviceSynchronize());
+    return split_device_status(p->t, 1);
+}
+
 // Host-buffer variants: chunks of the batch flow H2D (stream 0) -> compute (stream 1) -> D2H
 // (stream 2) through double-buffered device staging, so copies overlap the transforms.
 static int host_pipeline(s2g_plan p, int fwd, const float* in0, const float* in1, float* out0, float* out1,

@@ -97,5 +97,7 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
               cudaStream_t st);
 int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int batch, int precision, void* work,
                   cudaStream_t st);
+// Reads (and optionally clears) the device error word of the tensor-core kernels.
+int split_device_status(Tables* t, int clear);
 
 }  // namespace s2g

@@ -1,0 +1,142 @@
+"""Split-BF16 tensor-core path (tcgen05) vs the FP64 path and the oracle, through the C ABI.
+
+Error metric: normwise relative error max|x - x_ref| / max|x_ref| per function (coefficients
+for the forward, samples for the inverse), reference = FP64.  Stated tolerances:
+  S2G_PREC_BF16X3 (6 split products, FP32 FFT/DCT): <= 1e-6   (BASELINE headline tolerance)
+  S2G_PREC_BF16X2 (3 split products):               <= 1e-4
+"""
+import numpy as np
+import pytest
+
+from s2kit_gb300 import api
+from tests._util import real_field_coeffs
+
+pytestmark = pytest.mark.gpu
+TOL = {api.PREC_BF16X3: 1e-6, api.PREC_BF16X2: 1e-4}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+@pytest.mark.parametrize("n,k", [(16, 16), (64, 32), (128, 64), (256, 32), (32, 128)])
+def test_tc_selftest_tile(n, k):
+    torch = _torch()
+    g = torch.Generator(device="cpu").manual_seed(n * 1000 + k)
+    A = torch.randn(128, k, generator=g, dtype=torch.float32)
+    B = torch.randn(n, k, generator=g, dtype=torch.float32)
+    ref = A.double() @ B.double().T
+    dA, dB = A.cuda(), B.cuda()
+    scale = ref.abs().max().item()
+    errs = {}
+    for nprod in (1, 3, 6):
+        D = torch.zeros(128, n, dtype=torch.float32, device="cuda")
+        api.selftest_tc(dA, dB, D, nprod)
+        torch.cuda.synchronize()
+        errs[nprod] = (D.double().cpu() - ref).abs().max().item() / scale
+    assert errs[1] < 3e-2
+    assert errs[3] < 1e-4
+    assert errs[6] < 2e-6, errs
+
+
+def _fp64_pair(plan, rc, ic):
+    """FP64 grid of the coefficients and FP64 forward of that grid (device API)."""
+    torch = _torch()
+    nb = rc.shape[0]
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    grid = torch.zeros(nb, 4 * plan.bw ** 2, dtype=torch.float64, device="cuda")
+    plan.inv_fst(d_rc, d_ic, grid, None, nb, api.REAL)
+    o_rc, o_ic = torch.zeros_like(d_rc), torch.zeros_like(d_ic)
+    plan.fst(grid, None, o_rc, o_ic, nb, api.REAL)
+    torch.cuda.synchronize()
+    return grid, o_rc, o_ic
+
+
+def _nerr(got, ref):
+    torch = _torch()
+    d = (got.double() - ref).abs().amax(dim=1)
+    return (d / ref.abs().amax(dim=1)).max().item()
+
+
+@pytest.mark.parametrize("bw,nb", [(16, 3), (32, 70), (64, 10), (128, 65), (256, 130), (512, 2)])
+@pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_BF16X2])
+def test_split_forward_inverse_vs_fp64(bw, nb, prec):
+    torch = _torch()
+    rng = np.random.default_rng(bw + nb)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    grid64, frc64, fic64 = _fp64_pair(plan, rc, ic)
+    # forward: FP32 samples of the FP64 grid
+    g32 = grid64.float()
+    s_rc = torch.full((nb, bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+    s_ic = torch.full_like(s_rc, float("nan"))
+    plan.fst_real_f32(g32, s_rc, s_ic, nb, prec)
+    # inverse: FP32 coefficients
+    c32r, c32i = torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda()
+    s_grid = torch.full((nb, 4 * bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(c32r, c32i, s_grid, nb, prec)
+    plan.sync_status()
+    assert torch.isfinite(s_rc).all() and torch.isfinite(s_ic).all() and torch.isfinite(s_grid).all()
+    # coefficients compared as complex magnitudes
+    ref_mag = torch.hypot(frc64, fic64).amax(dim=1)
+    e_fwd = (torch.hypot(s_rc.double() - frc64, s_ic.double() - fic64).amax(dim=1) / ref_mag).max().item()
+    e_inv = _nerr(s_grid, grid64)
+    assert e_fwd <= TOL[prec], e_fwd
+    assert e_inv <= TOL[prec], e_inv
+
+
+def test_split_matches_oracle_and_roundtrip(oracle):
+    torch = _torch()
+    bw, nb = 64, 4
+    rng = np.random.default_rng(5)
+    rc, ic = real_field_coeffs(rng, bw, 1.5, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    c32r, c32i = torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda()
+    grid = torch.zeros(nb, 4 * bw * bw, dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(c32r, c32i, grid, nb, api.PREC_BF16X3)
+    o_rc, o_ic = torch.zeros_like(c32r), torch.zeros_like(c32i)
+    plan.fst_real_f32(grid, o_rc, o_ic, nb, api.PREC_BF16X3)
+    plan.sync_status()
+    g = grid.double().cpu().numpy()
+    for f in range(nb):
+        er, _ = oracle.inv_fst(rc[f], ic[f], bw, api.REAL, bw)
+        assert np.abs(g[f] - er).max() <= 1e-6 * np.abs(er).max()
+        mag = np.hypot(rc[f], ic[f]).max()
+        d = np.hypot(o_rc[f].double().cpu().numpy() - rc[f], o_ic[f].double().cpu().numpy() - ic[f]).max()
+        assert d <= 2e-6 * mag
+
+
+def test_split_host_api_matches_device_api():
+    torch = _torch()
+    bw, nb = 64, 150  # several pipeline chunks
+    rng = np.random.default_rng(9)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    rc32, ic32 = rc.astype(np.float32), ic.astype(np.float32)
+    plan = api.Plan(bw, bw)
+    grid_h = np.zeros((nb, 4 * bw * bw), dtype=np.float32)
+    plan.inv_fst_real_f32_host(rc32, ic32, grid_h, nb, api.PREC_BF16X3)
+    orc_h, oic_h = np.zeros_like(rc32), np.zeros_like(ic32)
+    plan.fst_real_f32_host(grid_h, orc_h, oic_h, nb, api.PREC_BF16X3)
+    d_grid = torch.zeros(nb, 4 * bw * bw, dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(torch.from_numpy(rc32).cuda(), torch.from_numpy(ic32).cuda(), d_grid, nb,
+                          api.PREC_BF16X3)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_grid.cpu().numpy(), grid_h)
+    d_rc = torch.zeros(nb, bw * bw, dtype=torch.float32, device="cuda")
+    d_ic = torch.zeros_like(d_rc)
+    plan.fst_real_f32(torch.from_numpy(grid_h).cuda(), d_rc, d_ic, nb, api.PREC_BF16X3)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_rc.cpu().numpy(), orc_h) and np.array_equal(d_ic.cpu().numpy(), oic_h)
+
+
+def test_split_rejects_unsupported():
+    import s2kit_gb300 as s2
+    torch = _torch()
+    plan = api.Plan(24, 24)  # not a power of two
+    x = torch.zeros(4 * 24 * 24, device="cuda")
+    with pytest.raises(s2.S2GError):
+        plan.fst_real_f32(x, x, x, 1, api.PREC_BF16X3)
+    plan64 = api.Plan(64, 64)
+    with pytest.raises(s2.S2GError):
+        plan64.fst_real_f32(x, x, x, 1, 7)  # unknown precision
