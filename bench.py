@@ -1,0 +1,443 @@
+#!/usr/bin/env python
+"""Benchmark: fwd+inv spherical harmonic transforms per second at bandwidth 256, batched.
+
+One step = InvFST of `batch` real fields (coefficients -> 512x512 samples) followed by FST
+of the result (samples -> coefficients), FP32 samples and coefficients, Legendre contraction
+as 3-term split BF16 on the tcgen05 tensor cores (S2G_PREC_BF16X3).  Synthetic seeded inputs:
+coefficients complex N(0,1)*(1+l)^-1 with the real-field symmetry.
+
+Reported on one JSON line (rank 0):
+  value         device-resident throughput (inputs in HBM), CUDA events on the stream
+  e2e           the same through the host-buffer C ABI (pinned host memory in/out)
+  fp64          the plain FP64 GPU path on the same workload, and the split/FP64 ratio
+  rel_err       normwise error of the split path vs the FP64 path (coefficients, samples)
+  roofline      dominant kernel: algorithmic bytes per launch / its event-timed duration
+  cpu_baseline  the CPU oracle port (oracle/s2oracle.c) on a bounded sample, all host cores
+  clocks        nvidia-smi samples taken while the GPU work ran
+`--impl reference` times the CPU implementation of the same path on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+inv SHT/sec at B=256 batched, split-BF16 vs plain FP64 on GB300 at rel err ≤1e-6"
+UNIT = "transforms/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--bw", type=int, default=256)
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=1234)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def real_field_coeffs(rng, bw, p, nfunc):
+    """Complex N(0,1)*(1+l)^-p, f(l,-m) = (-1)^m conj f(l,m), f(l,0) real (reference layout)."""
+    L = bw - 1
+    rc = np.zeros((nfunc, bw * bw))
+    ic = np.zeros((nfunc, bw * bw))
+    for m in range(bw):
+        l = np.arange(m, bw)
+        s = (1.0 + l) ** (-p)
+        x = rng.standard_normal((nfunc, l.size)) * s
+        y = rng.standard_normal((nfunc, l.size)) * s
+        if m == 0:
+            y[:] = 0.0
+        i0 = m * bw - (m * (m - 1)) // 2 + (l - m)
+        rc[:, i0], ic[:, i0] = x, y
+        if m:
+            i1 = (L * (L + 3)) // 2 + 1 + ((L - m) * (L - m + 1)) // 2 + (l - m)
+            sg = (-1.0) ** m
+            rc[:, i1], ic[:, i1] = sg * x, -sg * y
+    return rc, ic
+
+
+def config(args):
+    return {
+        "workload": f"real-field SHT fwd+inv, bandwidth {args.bw} ({2 * args.bw}x{2 * args.bw} Driscoll-Healy grid), "
+                    f"batch {args.batch} functions per GPU, FP32 samples and coefficients, seminaive Legendre "
+                    f"contraction as 3-term split BF16 on tcgen05 (FP32 accumulation)",
+        "bw": args.bw,
+        "batch_per_gpu": args.batch,
+        "spectrum": "complex N(0,1)*(1+l)^-1, real-field symmetry, seeded",
+        "l2": "inputs larger than L2 (coefficients %d MB + samples %d MB per step per GPU, L2 129 MB)" % (
+            args.batch * args.bw * args.bw * 8 // 2 ** 20, args.batch * 4 * args.bw * args.bw * 4 // 2 ** 20),
+        "parallelism": f"dp{args.gpus} (independent functions per GPU, no collective)",
+    }
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ["clocks.sm", "clocks.max.sm", "utilization.gpu", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), float(parts[2]), parts[4:]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        loaded = [r for r in rows if r[2] >= 50.0] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in loaded for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(loaded)}
+
+
+# --------------------------------------------------------------------------- roofline
+def algorithmic_bytes(kernel, B, N):
+    """Compulsory HBM bytes of one launch of `kernel` for N functions at bandwidth B (FP32)."""
+    S = 2 * B
+    nn = min(B, 32) // 2          # naive (odd m < 32) orders of the split path
+    ns = B - nn                   # seminaive orders
+    f = 4
+    table = {
+        "rows_fwd_f32": N * S * S * f + 2 * N * B * S * f,
+        "dct_fwd_f32": 2 * N * ns * S * f + 2 * N * ns * B * f,
+        "leg_tc_fwd": 2 * N * ns * B * f + 2 * N * nn * S * f + 2 * N * B * B * f,
+        "leg_tc_inv": 2 * N * (B * (B + 1) // 2) * f + 2 * N * ns * B * f + 2 * N * nn * S * f,
+        "dct_inv_f32": 2 * N * ns * B * f + 2 * N * ns * S * f,
+        "naive_combine_f32": 2 * 2 * N * nn * S * f,
+        "rows_inv_f32": 2 * N * B * S * f + N * S * S * f,
+    }
+    return table.get(kernel)
+
+
+def read_traffic(kernel, B, N):
+    """DRAM bytes per launch from the committed ncu summary of this kernel, if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_bw{B}.txt")
+    if not os.path.exists(path):
+        return None
+    scale = None
+    traffic = None
+    for ln in open(path):
+        if ln.startswith("dram_bytes_per_function:"):
+            traffic = float(ln.split(":")[1]) * N
+            scale = True
+    return traffic if scale else None
+
+
+# --------------------------------------------------------------------------- CPU legs
+def cpu_roundtrip(bw, nfunc, nthreads, seed):
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    rc, ic = real_field_coeffs(np.random.default_rng(seed), bw, 1.0, nfunc)
+    coeffs = np.stack([rc, ic], axis=1)
+    secs, _ = orc.bench_roundtrip(bw, coeffs, nthreads)
+    return secs
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    nfunc = 2 * nthreads
+    for _ in range(args.warmup):
+        cpu_roundtrip(args.bw, nfunc, nthreads, args.seed)
+    times = [cpu_roundtrip(args.bw, nfunc, nthreads, args.seed + i) for i in range(args.steps)]
+    total = sum(times)
+    value = nfunc * args.steps / total
+    sample = (f"{nfunc} functions per step (InvFST+FST, REAL, cutoff=bw), one function per thread, "
+              f"{nthreads} threads; the CPU restatement of the reference (oracle/s2oracle.c, gcc -O3, "
+              f"project radix-2 FFT in place of FFTW3); the reference sources themselves are not built on this host")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(args),
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- GPU arm
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    from s2kit_gb300 import api, load
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    lib = load()
+    B, N = args.bw, args.batch
+    S = 2 * B
+    rng = np.random.default_rng(args.seed + rank)
+    rc64, ic64 = real_field_coeffs(rng, B, 1.0, N)
+    d_rc = torch.from_numpy(rc64).float().cuda()
+    d_ic = torch.from_numpy(ic64).float().cuda()
+    grid = torch.empty(N, S * S, dtype=torch.float32, device="cuda")
+    o_rc = torch.empty_like(d_rc)
+    o_ic = torch.empty_like(d_ic)
+    plan = api.Plan(B, B)
+    stream = torch.cuda.current_stream()
+    prec = api.PREC_BF16X3
+
+    def step():
+        plan.inv_fst_real_f32(d_rc, d_ic, grid, N, prec, stream)
+        plan.fst_real_f32(grid, o_rc, o_ic, N, prec, stream)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    plan.sync_status()
+
+    # ---- timed region: device-resident split path
+    launches0 = lib.s2g_launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = lib.s2g_launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    value = ws * N / (ms / 1e3)
+    plan.sync_status()
+
+    # ---- per-kernel event timing pass (same steps, every launch bracketed by events)
+    import ctypes
+    nprof = max(3, min(args.steps, 50))
+    lib.s2g_prof_enable(1)
+    for _ in range(nprof):
+        step()
+    torch.cuda.synchronize()
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib.s2g_prof_report(buf, len(buf))
+    lib.s2g_prof_enable(0)
+    prof = json.loads(buf.value.decode())
+    kern = {k: {"launches": v[0], "avg_ms": v[1] / v[0], "total_ms": v[1]} for k, v in prof.items()}
+    tot = sum(v["total_ms"] for v in kern.values())
+    for v in kern.values():
+        v["share"] = v["total_ms"] / tot if tot else 0.0
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    ab = algorithmic_bytes(dom, B, N)
+    achieved = ab / (kern[dom]["avg_ms"] / 1e3) / 1e9 if ab else None
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": (achieved / hbm_peak) if achieved else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": ab, "traffic": read_traffic(dom, B, N),
+                "avg_launch_ms": kern[dom]["avg_ms"]}
+    # the tensor-core kernels against the measured bf16 peak (useful and issued flops)
+    tc = {}
+    for k in ("leg_tc_fwd", "leg_tc_inv"):
+        if k in kern:
+            issued = tc_flops_issued(B, N, k == "leg_tc_fwd", 6)
+            tc[k] = {"avg_ms": kern[k]["avg_ms"], "issued_tflops": issued / (kern[k]["avg_ms"] / 1e3) / 1e12,
+                     "useful_tflops": useful_flops(B, N) / (kern[k]["avg_ms"] / 1e3) / 1e12,
+                     "peak_tflops": peaks.get("bf16_tflops", 1900.0)}
+    all_bytes = sum((algorithmic_bytes(k, B, N) or 0) for k in kern)
+    step_gbs = all_bytes / (ms / 1e3) / 1e9
+
+    # ---- plain FP64 GPU path, same coefficients (FP64 copies)
+    d_rc64 = torch.from_numpy(rc64).cuda()
+    d_ic64 = torch.from_numpy(ic64).cuda()
+    grid64 = torch.empty(N, S * S, dtype=torch.float64, device="cuda")
+    o_rc64 = torch.empty_like(d_rc64)
+    o_ic64 = torch.empty_like(d_ic64)
+
+    def step64():
+        plan.inv_fst(d_rc64, d_ic64, grid64, None, N, api.REAL, stream)
+        plan.fst(grid64, None, o_rc64, o_ic64, N, api.REAL, stream)
+
+    step64()
+    torch.cuda.synchronize()
+    k64 = max(3, min(args.steps, 10))
+    e0.record(stream)
+    for _ in range(k64):
+        step64()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / k64
+    value64 = N / (ms64 / 1e3)
+
+    # ---- accuracy of the split path vs FP64 on this workload (same inputs)
+    step()
+    torch.cuda.synchronize()
+    mag = torch.hypot(o_rc64, o_ic64).amax(dim=1)
+    err_c = (torch.hypot(o_rc.double() - o_rc64, o_ic.double() - o_ic64).amax(dim=1) / mag).max().item()
+    err_g = ((grid.double() - grid64).abs().amax(dim=1) / grid64.abs().amax(dim=1)).max().item()
+    err_rt = (torch.hypot(o_rc.double() - torch.from_numpy(rc64).cuda(), o_ic.double() -
+                          torch.from_numpy(ic64).cuda()).amax(dim=1) / mag).max().item()
+    del d_rc64, d_ic64, grid64, o_rc64, o_ic64
+
+    # ---- end to end through the host-buffer C ABI (pinned host memory)
+    h_rc = torch.from_numpy(rc64).float().pin_memory().numpy()
+    h_ic = torch.from_numpy(ic64).float().pin_memory().numpy()
+    h_grid = torch.empty(N, S * S, dtype=torch.float32).pin_memory().numpy()
+    h_orc = torch.empty(N, B * B, dtype=torch.float32).pin_memory().numpy()
+    h_oic = torch.empty(N, B * B, dtype=torch.float32).pin_memory().numpy()
+
+    def step_e2e():
+        plan.inv_fst_real_f32_host(h_rc, h_ic, h_grid, N, prec)
+        plan.fst_real_f32_host(h_grid, h_orc, h_oic, N, prec)
+
+    step_e2e()
+    ke = max(3, min(args.steps, 20))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        step_e2e()
+    t1 = time.perf_counter()
+    ms_e2e = 1e3 * (t1 - t0) / ke
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = t.item()
+    e2e_value = ws * N / (ms_e2e / 1e3)
+    h2d = h_rc.nbytes + h_ic.nbytes + h_grid.nbytes
+    d2h = h_grid.nbytes + h_orc.nbytes + h_oic.nbytes
+    clk = clocks.stop()
+
+    # ---- CPU baseline (rank 0): bounded sample of the same workload on all host cores
+    cpu = None
+    if rank == 0:
+        nthreads = os.cpu_count() or 1
+        t1f = cpu_roundtrip(B, 1, 1, args.seed)
+        nfunc = int(max(nthreads, min(64 * nthreads, 10.0 / max(t1f, 1e-3))))
+        nfunc = ((nfunc + nthreads - 1) // nthreads) * nthreads
+        secs = cpu_roundtrip(B, nfunc, nthreads, args.seed)
+        cpu = {"value": nfunc / secs, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{nfunc} functions at bw {B} (InvFST+FST, REAL), {nthreads} threads, one function per "
+                         f"thread at a time, {secs:.2f} s wall; CPU restatement of the reference "
+                         f"(oracle/s2oracle.c, gcc -O3, radix-2 FFT in place of FFTW3)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32+bf16x3", "data": "synthetic", "config": config(args),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": ms_e2e, "timing": "host wall clock around the synchronous host-buffer calls"},
+            "gpu_launches": int(launches),
+            "fp64": {"value": value64, "unit": UNIT, "ms_per_step": ms64, "split_over_fp64": value / value64},
+            "rel_err": {"coeff_vs_fp64": err_c, "samples_vs_fp64": err_g, "roundtrip_vs_input": err_rt,
+                        "metric": "max over functions of max|x - x_fp64| / max|x_fp64|"},
+            "roofline": roofline,
+            "tensor": tc,
+            "step_hbm_gbs": step_gbs,
+            "kernels": kern,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def tc_flops_issued(B, N, fwd, nprod):
+    """MMA flops issued by one launch (dense padded tiles, all split products)."""
+    nn = min(B, 32) // 2
+    tot = 0
+    for m in range(B):
+        naive = (m & 1) and m < 32
+        nr0 = (B - m + 1) // 2
+        np_ = ((nr0 + 15) // 16) * 16
+        if fwd:
+            kx = B if naive else B // 2
+            n_ = np_
+        else:
+            kx = nr0
+            n_ = (min(B, 256) if naive else B // 2) * (B // min(B, 256) if naive else 1)
+        kpad = ((kx + 31) // 32) * 32
+        tot += 2 * 128 * n_ * kpad * 2 * nprod  # both parities, M = 128 rows
+    tiles = (N + 63) // 64
+    _ = nn
+    return tot * tiles
+
+
+def useful_flops(B, N):
+    """Seminaive Legendre flops of one direction: 4 * table entries per function (re + im)."""
+    table = 0
+    for m in range(B):
+        k = m // 2
+        # sum_{l=m}^{B-1} RowSize(m, l)
+        table += sum((l // 2 + 1) if m % 2 == 0 else ((l - 1) // 2 + 1) for l in range(m, B))
+        _ = k
+    return 4 * table * N
+
+
+if __name__ == "__main__":
+    main()

@@ -197,6 +197,15 @@ int s2g_plan_sync_status(s2g_plan plan);
  * of the six split products (1 = plain BF16 ... 6 = 3-term split).  Synchronous. */
 int s2g_selftest_tc(int N, int K, int nprod, const float* A, const float* B, float* D);
 
+/* Kernel timing: while enabled, every kernel the library launches is bracketed by CUDA
+ * events on the stream it is launched on.  s2g_prof_enable() also discards earlier records.
+ * s2g_prof_report() waits for the recorded events and writes a JSON object
+ * {"kernel": [launches, total_ms], ...} into buf. */
+int s2g_prof_enable(int on);
+int s2g_prof_report(char* buf, size_t len);
+/* Number of kernels the library has launched in this process. */
+unsigned long long s2g_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -33,6 +34,48 @@ int fail(int code, const char* fmt, ...) {
 int cuda_fail(cudaError_t e, const char* what) {
     return fail(e == cudaErrorMemoryAllocation ? S2G_ERR_NOMEM : S2G_ERR_CUDA, "%s: %s", what,
                 cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------------
+// Launch counting and optional per-kernel event timing.
+static std::atomic<unsigned long long> g_launches{0};
+static std::atomic<int> g_prof_on{0};
+struct ProfRec {
+    std::string name;
+    cudaEvent_t a, b;
+};
+static std::mutex g_prof_mu;
+static std::vector<ProfRec> g_prof_recs;
+static std::vector<cudaEvent_t> g_prof_pool;
+static thread_local std::vector<size_t> t_prof_open;
+
+static cudaEvent_t prof_event() {
+    if (!g_prof_pool.empty()) {
+        cudaEvent_t e = g_prof_pool.back();
+        g_prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void prof_begin(const char* name, cudaStream_t st) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    ProfRec r{name, prof_event(), prof_event()};
+    cudaEventRecord(r.a, st);
+    g_prof_recs.push_back(r);
+    t_prof_open.push_back(g_prof_recs.size() - 1);
+}
+
+void prof_end(cudaStream_t st) {
+    if (!g_prof_on.load(std::memory_order_relaxed) || t_prof_open.empty()) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    const size_t i = t_prof_open.back();
+    t_prof_open.pop_back();
+    if (i < g_prof_recs.size()) cudaEventRecord(g_prof_recs[i].b, st);
 }
 
 int Scratch::ensure(size_t need) {
@@ -845,5 +888,44 @@ int s2g_inv_fst_real_f32_host(s2g_plan p, const float* rc, const float* ic, floa
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
     return host_pipeline(p, 0, rc, ic, grid, nullptr, batch, precision);
 }
+
+int s2g_prof_enable(int on) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (auto& r : g_prof_recs) {
+        cudaEventSynchronize(r.b);
+        g_prof_pool.push_back(r.a);
+        g_prof_pool.push_back(r.b);
+    }
+    g_prof_recs.clear();
+    g_prof_on.store(on ? 1 : 0);
+    return S2G_OK;
+}
+
+int s2g_prof_report(char* buf, size_t len) {
+    if (!buf || len < 3) return fail(S2G_ERR_ARG, "report buffer too small");
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    std::map<std::string, std::pair<long, double>> agg;
+    for (auto& r : g_prof_recs) {
+        S2G_CUDA(cudaEventSynchronize(r.b));
+        float ms = 0.f;
+        S2G_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        auto& a = agg[r.name];
+        a.first += 1;
+        a.second += ms;
+    }
+    std::string out = "{";
+    for (auto& kv : agg) {
+        char tmp[256];
+        snprintf(tmp, sizeof(tmp), "%s\"%s\": [%ld, %.6f]", out.size() > 1 ? ", " : "", kv.first.c_str(),
+                 kv.second.first, kv.second.second);
+        out += tmp;
+    }
+    out += "}";
+    if (out.size() + 1 > len) return fail(S2G_ERR_ARG, "report buffer too small (%zu needed)", out.size() + 1);
+    memcpy(buf, out.c_str(), out.size() + 1);
+    return S2G_OK;
+}
+
+unsigned long long s2g_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"

@@ -28,6 +28,17 @@ int cuda_fail(cudaError_t e, const char* what);
         if (r_ != S2G_OK) return r_; \
     } while (0)
 
+// Kernel launch accounting: every launch is counted; when profiling is enabled
+// (s2g_prof_enable) it is also bracketed by CUDA events on its own stream.
+void prof_begin(const char* name, cudaStream_t st);
+void prof_end(cudaStream_t st);
+
+struct ProfScope {
+    cudaStream_t st;
+    ProfScope(const char* name, cudaStream_t s) : st(s) { prof_begin(name, s); }
+    ~ProfScope() { prof_end(st); }
+};
+
 // Device tables and constants for one (bandwidth, cutoff) on one device.
 struct Tables {
     int bw = 0, cutoff = 0, device = -1;

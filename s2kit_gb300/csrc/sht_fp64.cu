@@ -42,7 +42,10 @@ __global__ void k_twiddles(int n, double2* full, double2* quarter) {
 }
 
 int twiddles_device(int n, double2* d_full, double2* d_quarter, cudaStream_t st) {
-    k_twiddles<<<(n + 255) / 256, 256, 0, st>>>(n, d_full, d_quarter);
+    {
+        ProfScope ps_("twiddles", st);
+        k_twiddles<<<(n + 255) / 256, 256, 0, st>>>(n, d_full, d_quarter);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -427,7 +430,10 @@ static int launch_rows_fwd(const double* rdata, const double* idata, double* Xr,
     const size_t smem = rows_smem(S, R);
     S2G_TRY(set_smem((const void*)k_rows_fwd<double, double2>, smem));
     dim3 grid((S + lat_per - 1) / lat_per, batch);
-    k_rows_fwd<double, double2><<<grid, 256, smem, st>>>(rdata, idata, Xr, Xi, S, L.logn, rows_out, R, sqrt(2.0 * kPi) / S, tw);
+    {
+        ProfScope ps_("rows_fwd_f64", st);
+        k_rows_fwd<double, double2><<<grid, 256, smem, st>>>(rdata, idata, Xr, Xi, S, L.logn, rows_out, R, sqrt(2.0 * kPi) / S, tw);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -453,7 +459,10 @@ static int launch_fwd_dlt(FwdDlt p, int nrows_grid, cudaStream_t st) {
     p.logS = L.logn;
     S2G_TRY(set_smem((const void*)k_fwd_dlt, smem));
     dim3 grid(nrows_grid, (p.nfunc + G - 1) / G);
-    k_fwd_dlt<<<grid, 256, smem, st>>>(p);
+    {
+        ProfScope ps_("fwd_dlt_f64", st);
+        k_fwd_dlt<<<grid, 256, smem, st>>>(p);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -472,7 +481,10 @@ static int launch_inv_dlt(InvDlt p, int nrows_grid, cudaStream_t st) {
     p.logS = L.logn;
     S2G_TRY(set_smem((const void*)k_inv_dlt, smem));
     dim3 grid(nrows_grid, (p.nfunc + G - 1) / G);
-    k_inv_dlt<<<grid, 256, smem, st>>>(p);
+    {
+        ProfScope ps_("inv_dlt_f64", st);
+        k_inv_dlt<<<grid, 256, smem, st>>>(p);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -543,7 +555,10 @@ int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rda
     const size_t smem = rows_smem(S, R);
     S2G_TRY(set_smem((const void*)k_rows_inv<double, double2>, smem));
     dim3 grid((S + lat_per - 1) / lat_per, batch);
-    k_rows_inv<double, double2><<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L.logn, R, t->tw_S);
+    {
+        ProfScope ps_("rows_inv_f64", st);
+        k_rows_inv<double, double2><<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L.logn, R, t->tw_S);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -554,7 +569,10 @@ int fzt_f64(const Tables* t, const double* rdata, const double* idata, double* r
     double* Xr = (double*)work;
     double* Xi = Xr + (size_t)batch * S;
     dim3 g1((S + 7) / 8, batch);
-    k_rowsum<<<g1, 256, 0, st>>>(rdata, idata, Xr, Xi, S, sqrt(2.0 * kPi) / S);
+    {
+        ProfScope ps_("rowsum_f64", st);
+        k_rowsum<<<g1, 256, 0, st>>>(rdata, idata, Xr, Xi, S, sqrt(2.0 * kPi) / S);
+    }
     S2G_CUDA(cudaGetLastError());
     FwdDlt p{};
     p.Xr = Xr;
@@ -582,7 +600,10 @@ int fzt_f64(const Tables* t, const double* rdata, const double* idata, double* r
 int transmult_f64(const double* rd, const double* id, const double* rf, const double* iff, double* rr, double* ir,
                   int bw, int batch, cudaStream_t st) {
     dim3 grid(2 * bw - 1, batch);
-    k_transmult<<<grid, 128, 0, st>>>(rd, id, rf, iff, rr, ir, bw);
+    {
+        ProfScope ps_("transmult_f64", st);
+        k_transmult<<<grid, 128, 0, st>>>(rd, id, rf, iff, rr, ir, bw);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }

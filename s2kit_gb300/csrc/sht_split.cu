@@ -232,10 +232,22 @@ static int build_split(Tables* t) {
         ck(cudaMemcpyAsync(s->fwd_off, fo.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
         ck(cudaMemcpyAsync(s->inv_off, io.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
         ck(cudaMemcpyAsync(d_po, po.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
-        k_to_f32<<<(4 * B + 255) / 256, 256, 0, st>>>(t->weights, s->w32, 4 * B);
-        k_to_f32<<<(S + 255) / 256, 256, 0, st>>>(t->sinv, s->sin32, S);
-        k_tw_f32<<<(S + 255) / 256, 256, 0, st>>>(t->tw_S, s->twS, S);
-        k_tw_f32<<<(S + 255) / 256, 256, 0, st>>>(t->tw_D, s->twD, S);
+        {
+            ProfScope ps_("to_f32", st);
+            k_to_f32<<<(4 * B + 255) / 256, 256, 0, st>>>(t->weights, s->w32, 4 * B);
+        }
+        {
+            ProfScope ps_("to_f32", st);
+            k_to_f32<<<(S + 255) / 256, 256, 0, st>>>(t->sinv, s->sin32, S);
+        }
+        {
+            ProfScope ps_("tw_f32", st);
+            k_tw_f32<<<(S + 255) / 256, 256, 0, st>>>(t->tw_S, s->twS, S);
+        }
+        {
+            ProfScope ps_("tw_f32", st);
+            k_tw_f32<<<(S + 255) / 256, 256, 0, st>>>(t->tw_D, s->twD, S);
+        }
         ck(cudaGetLastError(), "conversion kernels");
     }
     // sampled P(m,l) of the naive orders (pml.c:41-79), one order at a time
@@ -247,7 +259,10 @@ static int build_split(Tables* t) {
         Pack pk{B, t->fwd, t->off, pml, d_po, t->weights, s->fwd_blob, s->fwd_off};
         int maxch = 0;
         for (int m = 0; m < B; ++m) maxch = std::max(maxch, geo(true, B, m).nch);
-        k_pack<true><<<dim3(B, maxch, 2), 256, 0, st>>>(pk);
+        {
+            ProfScope ps_("pack_fwd", st);
+            k_pack<true><<<dim3(B, maxch, 2), 256, 0, st>>>(pk);
+        }
         pk.blob = s->inv_blob;
         pk.blob_off = s->inv_off;
         maxch = 0;
@@ -256,7 +271,10 @@ static int build_split(Tables* t) {
             maxch = std::max(maxch, geo(false, B, m).nch);
             maxblk = std::max(maxblk, geo(false, B, m).nblk);
         }
-        k_pack<false><<<dim3(B, maxch, 2 * maxblk), 256, 0, st>>>(pk);
+        {
+            ProfScope ps_("pack_inv", st);
+            k_pack<false><<<dim3(B, maxch, 2 * maxblk), 256, 0, st>>>(pk);
+        }
         ck(cudaGetLastError(), "pack kernels");
         ck(cudaStreamSynchronize(st), "pack kernels");
     }
@@ -660,9 +678,15 @@ static int launch_leg(bool fwd, Leg& p, cudaStream_t st) {
     for (int m = 0; m < p.B; ++m) nblk = std::max(nblk, geo(fwd, p.B, m).nblk);
     dim3 grid(p.B, (p.N + 63) / 64, 2 * nblk);
     if (fwd)
-        k_leg_tc<true><<<grid, kTPB, smem, st>>>(p, stage);
+        {
+            ProfScope ps_("leg_tc_fwd", st);
+            k_leg_tc<true><<<grid, kTPB, smem, st>>>(p, stage);
+        }
     else
-        k_leg_tc<false><<<grid, kTPB, smem, st>>>(p, stage);
+        {
+            ProfScope ps_("leg_tc_inv", st);
+            k_leg_tc<false><<<grid, kTPB, smem, st>>>(p, stage);
+        }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -685,8 +709,11 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
         const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
         S2G_TRY(set_smem((const void*)k_rows_fwd<float, float2>, smem));
         dim3 grid2((S + 2 * R - 1) / (2 * R), batch);
-        k_rows_fwd<float, float2><<<grid2, 256, smem, st>>>(grid, nullptr, X, X + (size_t)batch * B * S, S, L.logn, B,
-                                                           R, (float)(sqrt(2.0 * kPi) / S), s->twS);
+        {
+            ProfScope ps_("rows_fwd_f32", st);
+            k_rows_fwd<float, float2><<<grid2, 256, smem, st>>>(grid, nullptr, X, X + (size_t)batch * B * S, S, L.logn, B,
+                                                               R, (float)(sqrt(2.0 * kPi) / S), s->twS);
+        }
         S2G_CUDA(cudaGetLastError());
     }
     // 2. weighted DCT-II per (function, seminaive order)
@@ -695,7 +722,10 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
         const int R = dct_rows_per_cta(S);
         const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
         S2G_TRY(set_smem((const void*)k_dct_fwd32, smem));
-        k_dct_fwd32<<<(nrows + R - 1) / R, 256, smem, st>>>(X, Cb, nrows, B, L.logn, R, s->w32, s->twS, s->twD);
+        {
+            ProfScope ps_("dct_fwd_f32", st);
+            k_dct_fwd32<<<(nrows + R - 1) / R, 256, smem, st>>>(X, Cb, nrows, B, L.logn, R, s->w32, s->twS, s->twD);
+        }
         S2G_CUDA(cudaGetLastError());
     }
     // 3. tensor-core contraction (seminaive orders from C, naive orders from X)
@@ -741,11 +771,17 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
         const int R = dct_rows_per_cta(S);
         const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
         S2G_TRY(set_smem((const void*)k_dct_inv32, smem));
-        k_dct_inv32<<<(nrows + R - 1) / R, 256, smem, st>>>(Fc, F, nrows, B, L.logn, R, s->sin32, s->twS, s->twD,
-                                                             scale);
+        {
+            ProfScope ps_("dct_inv_f32", st);
+            k_dct_inv32<<<(nrows + R - 1) / R, 256, smem, st>>>(Fc, F, nrows, B, L.logn, R, s->sin32, s->twS, s->twD,
+                                                                 scale);
+        }
         S2G_CUDA(cudaGetLastError());
         const int nnaive = std::min(B, kNaiveOddBelow) / 2;
-        k_naive_combine<<<dim3(batch * nnaive, 2), 256, S * sizeof(float), st>>>(F, batch, B, scale);
+        {
+            ProfScope ps_("naive_combine_f32", st);
+            k_naive_combine<<<dim3(batch * nnaive, 2), 256, S * sizeof(float), st>>>(F, batch, B, scale);
+        }
         S2G_CUDA(cudaGetLastError());
     }
     {
@@ -753,8 +789,11 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
         const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
         S2G_TRY(set_smem((const void*)k_rows_inv<float, float2>, smem));
         dim3 grid2((S + 2 * R - 1) / (2 * R), batch);
-        k_rows_inv<float, float2><<<grid2, 256, smem, st>>>(F, F + (size_t)batch * B * S, B, 0, grid, nullptr, S,
-                                                           L.logn, R, s->twS);
+        {
+            ProfScope ps_("k_rows_inv<float, float2>", st);
+            k_rows_inv<float, float2><<<grid2, 256, smem, st>>>(F, F + (size_t)batch * B * S, B, 0, grid, nullptr, S,
+                                                               L.logn, R, s->twS);
+        }
         S2G_CUDA(cudaGetLastError());
     }
     return S2G_OK;
@@ -849,7 +888,10 @@ extern "C" int s2g_selftest_tc(int N, int K, int nprod, const float* dA, const f
     S2G_CUDA(cudaMemset(err, 0, sizeof(int)));
     const size_t smem = 1024 + 3 * (128 * (size_t)K * 2) + 3 * ((size_t)N * K * 2);
     S2G_TRY(set_smem((const void*)k_tc_selftest, smem));
-    k_tc_selftest<<<1, 128, smem>>>(N, K, nprod, dA, dB, dD, err);
+    {
+        ProfScope ps_("tc_selftest", 0);
+        k_tc_selftest<<<1, 128, smem>>>(N, K, nprod, dA, dB, dD, err);
+    }
     S2G_CUDA(cudaGetLastError());
     int v = 0;
     S2G_CUDA(cudaMemcpy(&v, err, sizeof(int), cudaMemcpyDeviceToHost));

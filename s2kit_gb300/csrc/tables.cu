@@ -225,19 +225,28 @@ __global__ void k_pmm(int m, const double* eval, int n, double* out) {
 
 // ------------------------------------------------------------------------------------
 int generate_weights_device(int bw, double* d_w, cudaStream_t st) {
-    k_weights<<<(2 * bw + 127) / 128, 128, 0, st>>>(bw, d_w);
+    {
+        ProfScope ps_("weights", st);
+        k_weights<<<(2 * bw + 127) / 128, 128, 0, st>>>(bw, d_w);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
 
 int nodes_device(int n, double* d_out, int mode, cudaStream_t st) {
-    k_nodes<<<(n + 255) / 256, 256, 0, st>>>(n, d_out, mode);
+    {
+        ProfScope ps_("nodes", st);
+        k_nodes<<<(n + 255) / 256, 256, 0, st>>>(n, d_out, mode);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
 
 int pmm_device(int m, const double* d_eval, int n, double* d_out, cudaStream_t st) {
-    k_pmm<<<(n + 255) / 256, 256, 0, st>>>(m, d_eval, n, d_out);
+    {
+        ProfScope ps_("pmm", st);
+        k_pmm<<<(n + 255) / 256, 256, 0, st>>>(m, d_eval, n, d_out);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -266,7 +275,10 @@ int generate_cos_pml_device(int bw, int m_begin, int m_end, double* d_fwd, const
     const size_t smem = (size_t)(7 * bw + 2 * bw) * sizeof(double);
     if (smem > 48 * 1024)
         S2G_CUDA(cudaFuncSetAttribute((const void*)k_gen_cos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_gen_cos<<<m_end - m_begin, 256, smem, st>>>(p);
+    {
+        ProfScope ps_("gen_cos_pml", st);
+        k_gen_cos<<<m_end - m_begin, 256, smem, st>>>(p);
+    }
     S2G_CUDA(cudaGetLastError());
     S2G_CUDA(cudaStreamSynchronize(st));  // twiddle buffers are freed on return
     return S2G_OK;
@@ -276,7 +288,10 @@ int transpose_cos_pml_device(int bw, int m_begin, int m_end, const double* d_fwd
                              const int64_t* d_off, cudaStream_t st) {
     if (m_end <= m_begin) return S2G_OK;
     const size_t smem = (size_t)(bw + 1 + 32) * sizeof(int);
-    k_transpose<<<m_end - m_begin, 256, smem, st>>>(bw, m_begin, d_fwd, d_inv, d_off);
+    {
+        ProfScope ps_("transpose_cos_pml", st);
+        k_transpose<<<m_end - m_begin, 256, smem, st>>>(bw, m_begin, d_fwd, d_inv, d_off);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -286,7 +301,10 @@ int generate_pml_device(int bw, int m_begin, int m_end, double* d_fwd, const int
     const size_t smem = (size_t)3 * 2 * bw * sizeof(double);
     if (smem > 48 * 1024)
         S2G_CUDA(cudaFuncSetAttribute((const void*)k_gen_pml, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_gen_pml<<<m_end - m_begin, 256, smem, st>>>(bw, m_begin, d_fwd, d_off);
+    {
+        ProfScope ps_("gen_pml", st);
+        k_gen_pml<<<m_end - m_begin, 256, smem, st>>>(bw, m_begin, d_fwd, d_off);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
