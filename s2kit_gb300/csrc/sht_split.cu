@@ -2,8 +2,8 @@
 // contraction on the 5th-generation tensor cores as split-BF16 products (FP32 accumulation in TMEM).
 //
 // Forward (FSTSemiMemo, REAL, cutoff = bw; FST_semi_memo.c:68-145):
-//   k_rows_fwd<float>  : DFT along phi, two real latitudes per complex DFT, X[p][f][m][theta]
-//   k_dct_fwd32        : weights (even/odd order) + REDFT10 + normalisation (seminaive.c:161-176)
+//   k_rows_fwd_w       : DFT along phi (warp FFT, two real latitudes per warp), X[p][f][m][theta]
+//   k_dct_fwd_w        : weights (even/odd order) + REDFT10 + normalisation (seminaive.c:161-176)
 //                        -> C[p][f][m][k], k < bw
 //   k_leg_fwd_tc       : per (order m, 64 functions): for each parity t of (l - m), the dense
 //                        trapezoid T_{m,t}[i][j] = T(m, l = m+t+2i, k = 2j+t) times C (seminaive.c:183-197)
@@ -11,8 +11,9 @@
 //                        (re, im) rows, B = table rows; epilogue writes f(l, m) and f(l, -m).
 // Inverse (InvFSTSemiMemo, REAL; FST_semi_memo.c:228-351):
 //   k_leg_inv_tc       : fcos[2j+t] = sum_i T_{m,t}[i][j] a(m + t + 2i) (seminaive.c:74-98), scaled
-//   k_dct_inv32        : REDFT01, sin(theta) for odd m, 1/sqrt(2 pi)
-//   k_rows_inv<float>  : DFT with sign +1 over m, Hermitian rows, two latitudes per DFT
+//   k_dct_inv_w        : REDFT01, sin(theta) for odd m, 1/sqrt(2 pi)
+//   k_naive_combine    : naive orders (odd m < 32): even/odd latitude halves back to samples
+//   k_rows_inv_w       : DFT with sign +1 over m, Hermitian rows, two latitudes per warp
 //
 // Precision: x = x0 + x1 + x2 with BF16 terms (each the rounded residual of the previous);
 // the table is split the same way from FP64.  S2G_PREC_BF16X3 sums the six products
@@ -25,9 +26,9 @@
 #include <mutex>
 #include <vector>
 
-#include "rows.cuh"
 #include "s2g_common.cuh"
 #include "s2g_internal.h"
+#include "fft32.cuh"
 #include "tc_sm103.cuh"
 
 namespace s2g {
@@ -77,7 +78,7 @@ static constexpr int kNaiveOddBelow = 32;
 __host__ __device__ __forceinline__ bool naive_order(int m) { return (m & 1) && m < kNaiveOddBelow; }
 
 static constexpr int kKC = 32;   // K columns per pipeline chunk (two K=16 MMA steps)
-static constexpr int kNBN = 256; // latitude block of the naive inverse (N per CTA)
+static constexpr int kNBN = 128; // latitude block of the naive inverse (N per CTA)
 
 // Geometry of the tensor-core contraction for one (direction, order): rows of the table
 // operand per CTA (N), K extent, K chunks and latitude blocks.
@@ -287,83 +288,250 @@ static int build_split(Tables* t) {
 }
 
 // ------------------------------------------------------------------------------------
-// FP32 DCTs over latitude for R (function, order) rows per CTA; rows of naive orders are
-// skipped (their Legendre transform reads / writes latitude samples directly).
-__global__ void k_dct_fwd32(const float* __restrict__ X, float* __restrict__ Cout, int nrows, int B, int logS, int R,
-                            const float* __restrict__ w, const float2* __restrict__ twS,
-                            const float2* __restrict__ twD) {
-    extern __shared__ __align__(16) float fsm[];
-    const int S = 2 * B;
-    const Len L{S, logS};
-    const int SP = S + 1;
-    float* zr = fsm;
-    float* zi = zr + (size_t)R * SP;
-    const int row0 = blockIdx.x * R;
-    const int nr = min(R, nrows - row0);
-    const size_t plane = (size_t)nrows * S;
-    for (int e = threadIdx.x; e < nr * S; e += blockDim.x) {
-        const int r = e / S, q = e - r * S;
-        const int m = (row0 + r) % B;
-        const float wq = w[q + ((m & 1) ? S : 0)];
-        const int d = (q & 1) ? S - 1 - (q >> 1) : (q >> 1);
-        const size_t src = (size_t)(row0 + r) * S + q;
-        const bool skip = naive_order(m);
-        zr[r * SP + L.pos(d)] = skip ? 0.f : X[src] * wq;
-        zi[r * SP + L.pos(d)] = skip ? 0.f : X[plane + src] * wq;
-    }
-    __syncthreads();
-    block_dft<float, float2>(zr, zi, L, nr, SP, twS, -1.0f, nullptr);
-    const float nrm = (float)(1.0 / sqrt(2.0 * S));
-    const float nrm0 = (float)(0.70710678118654752440 / sqrt(2.0 * S));
-    const size_t cplane = (size_t)nrows * B;
-    for (int e = threadIdx.x; e < nr * B; e += blockDim.x) {
-        const int r = e / B, k = e - r * B;
-        if (naive_order((row0 + r) % B)) continue;
-        const int kk = (k == 0) ? 0 : S - k;
-        const float ar = zr[r * SP + k], ai = zi[r * SP + k], br = zr[r * SP + kk], bi = zi[r * SP + kk];
-        const float c = twD[k].x, s = twD[k].y;
-        const float f = (k == 0) ? nrm0 : nrm;
-        Cout[(size_t)(row0 + r) * B + k] = ((ar + br) * c + (ai - bi) * s) * f;
-        Cout[cplane + (size_t)(row0 + r) * B + k] = ((ai + bi) * c - (ar - br) * s) * f;
+// Warp-FFT kernels (fft32.cuh), S = 2B = 32 R.  One warp owns one complex sequence; layout
+// changes go through padded shared memory.
+
+// Loads tw[k] = exp(2 pi i k / S), twD[k] = (cos, sin)(pi k / 2S) for k < S into shared memory.
+// (tw padded as padtw(k), see fft32.cuh; twD unpadded)
+__device__ __forceinline__ void load_tw(float2* tw, float2* twD, const float2* gS, const float2* gD, int S) {
+    for (int k = threadIdx.x; k < S; k += blockDim.x) {
+        tw[padtw(k)] = gS[k];
+        if (twD) twD[k] = gD[k];
     }
 }
 
-__global__ void k_dct_inv32(const float* __restrict__ Fc, float* __restrict__ F, int nrows, int B, int logS, int R,
-                            const float* __restrict__ sinv, const float2* __restrict__ twS,
-                            const float2* __restrict__ twD, float scale) {
+static constexpr int kWarps = 8;       // warps per CTA in the FFT kernels
+static constexpr int kLatPerCta = 16;  // latitudes per CTA in the row kernels (2 per warp)
+
+// DFT along phi of 16 latitudes (two real rows per warp), transposed to X[p][f][m][theta], m < B.
+template <int R>
+__global__ void __launch_bounds__(256) k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N,
+                                                    float scale, const float2* __restrict__ gtw) {
+    constexpr int S = 32 * R, B = S / 2;
+    constexpr int PS = S + S / 32;        // padded spectrum length
+    constexpr int RS = B + B / 32 + 1;    // padded stage row (odd)
+    constexpr int TWL = twtab_len(S);
     extern __shared__ __align__(16) float fsm[];
-    const int S = 2 * B;
-    const Len L{S, logS};
-    const int SP = S + 1;
-    float* zr = fsm;
-    float* zi = zr + (size_t)R * SP;
-    const int row0 = blockIdx.x * R;
-    const int nr = min(R, nrows - row0);
-    const size_t cplane = (size_t)nrows * B;
-    for (int e = threadIdx.x; e < nr * S; e += blockDim.x) {
-        const int r = e / S, k = e - r * S;
-        const bool skip = naive_order((row0 + r) % B);
-        const float* xa = Fc + (size_t)(row0 + r) * B;
-        const float* xb = xa + cplane;
-        const float ak = (!skip && k < B) ? xa[k] : 0.f, bk = (!skip && k < B) ? xb[k] : 0.f;
-        const int q = S - k;
-        const float ar = (!skip && k > 0 && q < B) ? xa[q] : 0.f, br = (!skip && k > 0 && q < B) ? xb[q] : 0.f;
-        const float wr = ak + br, wi = bk - ar;
-        const float c = twD[k].x, s = twD[k].y;
-        zr[r * SP + L.pos(k)] = wr * c - wi * s;
-        zi[r * SP + L.pos(k)] = wr * s + wi * c;
+    float2* tw = reinterpret_cast<float2*>(fsm);
+    float* spr = fsm + 2 * TWL;                    // [warps][PS] re
+    float* spi = spr + kWarps * PS;                // [warps][PS] im
+    float* str = spi + kWarps * PS;                // [16][RS] re
+    float* sti = str + kLatPerCta * RS;            // [16][RS] im
+    const int f = blockIdx.y, th0 = blockIdx.x * kLatPerCta;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    load_tw(tw, nullptr, gtw, nullptr, S);
+    __syncthreads();
+    const int la = th0 + 2 * warp;
+    if (la < S) {
+        const float* ra = grid + ((size_t)f * S + la) * S;
+        const float* rb = ra + S;
+        float2 v[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) v[i] = make_float2(ra[lane + 32 * i], (la + 1 < S) ? rb[lane + 32 * i] : 0.f);
+        WarpFFT<R>::run(v, tw, -1.f);
+        float* wr = spr + warp * PS;
+        float* wi = spi + warp * PS;
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) {
+            const int o = pad32(WarpFFT<R>::out_index(k1));
+            wr[o] = v[k1].x;
+            wi[o] = v[k1].y;
+        }
+        __syncwarp();
+        for (int m = lane; m < B; m += 32) {
+            const int mm = (S - m) & (S - 1);
+            const float zr = wr[pad32(m)], zi = wi[pad32(m)], xr = wr[pad32(mm)], xi = wi[pad32(mm)];
+            str[(2 * warp) * RS + pad32(m)] = 0.5f * (zr + xr) * scale;
+            sti[(2 * warp) * RS + pad32(m)] = 0.5f * (zi - xi) * scale;
+            str[(2 * warp + 1) * RS + pad32(m)] = 0.5f * (zi + xi) * scale;
+            sti[(2 * warp + 1) * RS + pad32(m)] = -0.5f * (zr - xr) * scale;
+        }
     }
     __syncthreads();
-    block_dft<float, float2>(zr, zi, L, nr, SP, twS, 1.0f, nullptr);
-    const size_t plane = (size_t)nrows * S;
-    for (int e = threadIdx.x; e < nr * S; e += blockDim.x) {
-        const int r = e / S, q = e - r * S;
-        const int m = (row0 + r) % B;
-        if (naive_order(m)) continue;
+    const int nlat = min(kLatPerCta, S - th0);
+    const size_t plane = (size_t)N * B * S;
+    for (int e = threadIdx.x; e < B * kLatPerCta; e += blockDim.x) {
+        const int m = e / kLatPerCta, q = e - m * kLatPerCta;
+        if (q >= nlat) continue;
+        const size_t o = ((size_t)f * B + m) * S + th0 + q;
+        X[o] = str[q * RS + pad32(m)];
+        X[plane + o] = sti[q * RS + pad32(m)];
+    }
+}
+
+// Weighted REDFT10 per (function, seminaive order) row: C[p][f][m][k], k < B.
+template <int R>
+__global__ void __launch_bounds__(256) k_dct_fwd_w(const float* __restrict__ X, float* __restrict__ Cout, int nrows,
+                                                   const float* __restrict__ gw, const float2* __restrict__ gtw,
+                                                   const float2* __restrict__ gtwD) {
+    constexpr int S = 32 * R, B = S / 2;
+    constexpr int PS = S + S / 32;
+    constexpr int TWL = twtab_len(S);
+    extern __shared__ __align__(16) float fsm[];
+    float2* tw = reinterpret_cast<float2*>(fsm);
+    float2* twD = tw + TWL;
+    float* w = fsm + 2 * TWL + 2 * S;    // 2S weights (even orders, then odd)
+    float* spr = w + 2 * S;
+    float* spi = spr + kWarps * PS;
+    load_tw(tw, twD, gtw, gtwD, S);
+    for (int q = threadIdx.x; q < 2 * S; q += blockDim.x) w[q] = gw[q];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * kWarps + warp;
+    if (row >= nrows) return;
+    const int m = row % B;
+    if (naive_order(m)) return;
+    const float* ws = w + ((m & 1) ? S : 0);
+    const float* xr = X + (size_t)row * S;
+    const float* xi = xr + (size_t)nrows * S;
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int j = lane + 32 * i;                        // v[j] = x[2j] | x[2(S-1-j)+1]
+        const int q = (j < S / 2) ? 2 * j : 2 * (S - 1 - j) + 1;
+        v[i] = make_float2(xr[q] * ws[q], xi[q] * ws[q]);
+    }
+    WarpFFT<R>::run(v, tw, -1.f);
+    float* wr = spr + warp * PS;
+    float* wi = spi + warp * PS;
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        const int o = pad32(WarpFFT<R>::out_index(k1));
+        wr[o] = v[k1].x;
+        wi[o] = v[k1].y;
+    }
+    __syncwarp();
+    const float nrm = rsqrtf(2.f * S);
+    const float nrm0 = 0.70710678118654752440f * nrm;
+    float* cr = Cout + (size_t)row * B;
+    float* ci = cr + (size_t)nrows * B;
+    for (int k = lane; k < B; k += 32) {
+        const int kk = (S - k) & (S - 1);
+        const float ar = wr[pad32(k)], ai = wi[pad32(k)], br = wr[pad32(kk)], bi = wi[pad32(kk)];
+        const float c = twD[k].x, sn = twD[k].y;
+        const float fct = (k == 0) ? nrm0 : nrm;
+        cr[k] = ((ar + br) * c + (ai - bi) * sn) * fct;
+        ci[k] = ((ai + bi) * c - (ar - br) * sn) * fct;
+    }
+}
+
+// REDFT01 per (function, seminaive order) row, sin(theta) for odd m, scale: F[p][f][m][theta].
+template <int R>
+__global__ void __launch_bounds__(256) k_dct_inv_w(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
+                                                   const float* __restrict__ gsin, const float2* __restrict__ gtw,
+                                                   const float2* __restrict__ gtwD, float scale) {
+    constexpr int S = 32 * R, B = S / 2;
+    constexpr int PS = S + S / 32;
+    constexpr int TWL = twtab_len(S);
+    extern __shared__ __align__(16) float fsm[];
+    float2* tw = reinterpret_cast<float2*>(fsm);
+    float2* twD = tw + TWL;
+    float* sn = fsm + 2 * TWL + 2 * S;
+    float* spr = sn + S;
+    float* spi = spr + kWarps * PS;
+    load_tw(tw, twD, gtw, gtwD, S);
+    for (int q = threadIdx.x; q < S; q += blockDim.x) sn[q] = gsin[q];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * kWarps + warp;
+    if (row >= nrows) return;
+    const int m = row % B;
+    if (naive_order(m)) return;
+    const float* xa = Fc + (size_t)row * B;
+    const float* xb = xa + (size_t)nrows * B;
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int k = lane + 32 * i;
+        const int r = S - k;
+        const float ak = (k < B) ? xa[k] : 0.f, bk = (k < B) ? xb[k] : 0.f;
+        const float ar = (k > 0 && r < B) ? xa[r] : 0.f, br = (k > 0 && r < B) ? xb[r] : 0.f;
+        const float wr = ak + br, wi = bk - ar;
+        const float2 d = twD[k];
+        v[i] = make_float2(wr * d.x - wi * d.y, wr * d.y + wi * d.x);
+    }
+    WarpFFT<R>::run(v, tw, 1.f);
+    float* zr = spr + warp * PS;
+    float* zi = spi + warp * PS;
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        const int o = pad32(WarpFFT<R>::out_index(k1));
+        zr[o] = v[k1].x;
+        zi[o] = v[k1].y;
+    }
+    __syncwarp();
+    float* fr = F + (size_t)row * S;
+    float* fi = fr + (size_t)nrows * S;
+    const bool odd = m & 1;
+    for (int q = lane; q < S; q += 32) {
         const int src = (q & 1) ? S - 1 - (q >> 1) : (q >> 1);
-        const float g = (m & 1) ? sinv[q] * scale : scale;
-        F[(size_t)(row0 + r) * S + q] = zr[r * SP + src] * g;
-        F[plane + (size_t)(row0 + r) * S + q] = zi[r * SP + src] * g;
+        const float g = odd ? sn[q] * scale : scale;
+        fr[q] = zr[pad32(src)] * g;
+        fi[q] = zi[pad32(src)] * g;
+    }
+}
+
+// DFT with sign +1 over the orders for 16 latitudes (two real output rows per warp).
+template <int R>
+__global__ void __launch_bounds__(256) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
+                                                    const float2* __restrict__ gtw) {
+    constexpr int S = 32 * R, B = S / 2;
+    constexpr int PS = S + S / 32;
+    constexpr int TS = kLatPerCta + 1;  // padded tile row (odd)
+    constexpr int TWL = twtab_len(S);
+    extern __shared__ __align__(16) float fsm[];
+    float2* tw = reinterpret_cast<float2*>(fsm);
+    float* tr = fsm + 2 * TWL;           // [B][TS]
+    float* ti = tr + B * TS;
+    float* spr = ti + B * TS;            // [warps][PS]
+    float* spi = spr + kWarps * PS;
+    const int f = blockIdx.y, th0 = blockIdx.x * kLatPerCta;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    load_tw(tw, nullptr, gtw, nullptr, S);
+    const int nlat = min(kLatPerCta, S - th0);
+    const size_t plane = (size_t)N * B * S;
+    for (int e = threadIdx.x; e < B * kLatPerCta; e += blockDim.x) {
+        const int m = e / kLatPerCta, q = e - m * kLatPerCta;
+        const size_t o = ((size_t)f * B + m) * S + th0 + q;
+        tr[m * TS + q] = (q < nlat) ? F[o] : 0.f;
+        ti[m * TS + q] = (q < nlat) ? F[plane + o] : 0.f;
+    }
+    __syncthreads();
+    const int a = 2 * warp, b = a + 1;
+    if (th0 + a >= S) return;
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int m = lane + 32 * i;
+        float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
+        if (m < B) {
+            ar = tr[m * TS + a];
+            ai = (m == 0) ? 0.f : ti[m * TS + a];
+            br = tr[m * TS + b];
+            bi = (m == 0) ? 0.f : ti[m * TS + b];
+        } else if (m > B) {
+            const int mm = S - m;
+            ar = tr[mm * TS + a];
+            ai = -ti[mm * TS + a];
+            br = tr[mm * TS + b];
+            bi = -ti[mm * TS + b];
+        }
+        v[i] = make_float2(ar - bi, ai + br);  // F_a + i F_b
+    }
+    WarpFFT<R>::run(v, tw, 1.f);
+    float* zr = spr + warp * PS;
+    float* zi = spi + warp * PS;
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        const int o = pad32(WarpFFT<R>::out_index(k1));
+        zr[o] = v[k1].x;
+        zi[o] = v[k1].y;
+    }
+    __syncwarp();
+    float* ga = grid + ((size_t)f * S + th0 + a) * S;
+    for (int k = lane; k < S; k += 32) {
+        ga[k] = zr[pad32(k)];
+        if (th0 + b < S) ga[S + k] = zi[pad32(k)];
     }
 }
 
@@ -474,22 +642,36 @@ __device__ __forceinline__ void load_seg(const Leg& p, int m, bool nv, int t, in
     }
 }
 
+// A operand of one chunk, split into loads (issued early, held in registers across the
+// barrier and the MMA issue of the previous chunk) and the BF16 split + shared-memory store.
+static constexpr int kTasks = 128 * (kKC / 8) / kTPB;  // (row, 8-column segment) tasks per thread
+
 template <bool FWD>
-__device__ __forceinline__ void produce_a(const Leg& p, uint8_t* st, int m, bool nv, int t, int f0, int c) {
+__device__ __forceinline__ void load_a(const Leg& p, int m, bool nv, int t, int f0, int c, float (&v)[kTasks][8]) {
     constexpr int segs = kKC / 8;
-    for (int task = threadIdx.x; task < 128 * segs; task += kTPB) {
+#pragma unroll
+    for (int q = 0; q < kTasks; ++q) {
+        const int task = threadIdx.x + q * kTPB;
         const int r = task / segs, seg = task - r * segs;
-        float v[8];
-        load_seg<FWD>(p, m, nv, t, f0 + (r & 63), r >> 6, c, seg, v);
+        load_seg<FWD>(p, m, nv, t, f0 + (r & 63), r >> 6, c, seg, v[q]);
+    }
+}
+
+__device__ __forceinline__ void store_a(uint8_t* st, const float (&v)[kTasks][8]) {
+    constexpr int segs = kKC / 8;
+#pragma unroll
+    for (int q = 0; q < kTasks; ++q) {
+        const int task = threadIdx.x + q * kTPB;
+        const int r = task / segs, seg = task - r * segs;
         uint32_t w[3][4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int j = 0; j < 4; ++j) {
             __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-            tc::split3(v[2 * q], a0, a1, a2);
-            tc::split3(v[2 * q + 1], b0, b1, b2);
-            w[0][q] = (uint32_t)__bfloat16_as_ushort(a0) | ((uint32_t)__bfloat16_as_ushort(b0) << 16);
-            w[1][q] = (uint32_t)__bfloat16_as_ushort(a1) | ((uint32_t)__bfloat16_as_ushort(b1) << 16);
-            w[2][q] = (uint32_t)__bfloat16_as_ushort(a2) | ((uint32_t)__bfloat16_as_ushort(b2) << 16);
+            tc::split3(v[q][2 * j], a0, a1, a2);
+            tc::split3(v[q][2 * j + 1], b0, b1, b2);
+            w[0][j] = (uint32_t)__bfloat16_as_ushort(a0) | ((uint32_t)__bfloat16_as_ushort(b0) << 16);
+            w[1][j] = (uint32_t)__bfloat16_as_ushort(a1) | ((uint32_t)__bfloat16_as_ushort(b1) << 16);
+            w[2][j] = (uint32_t)__bfloat16_as_ushort(a2) | ((uint32_t)__bfloat16_as_ushort(b2) << 16);
         }
         const uint32_t o = tc::tile_off(r, seg * 8, kKC);
 #pragma unroll
@@ -517,8 +699,10 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
     __shared__ uint32_t tmem_slot;
     __shared__ int s_abort;
     const int B = p.B;
-    const int m = blockIdx.x, f0 = blockIdx.y * 64;
-    const int t = blockIdx.z & 1, nb = blockIdx.z >> 1;
+    // parity is the fastest grid index: the two CTAs that write the interleaved (stride-2)
+    // halves of the same coefficient rows run back to back, so their sectors merge in L2
+    const int t = blockIdx.x & 1, nb = blockIdx.x >> 1;
+    const int m = blockIdx.y, f0 = blockIdx.z * 64;
     const Geo g = geo(FWD, B, m);
     if (nb >= g.nblk) return;  // uniform per CTA, before any barrier or TMEM use
     const bool nv = naive_order(m);
@@ -545,6 +729,8 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
     const uint32_t idesc = tc::idesc_bf16_f32(128, NP);
     constexpr uint32_t sbo = (kKC / 8) * 128;
 
+    float va[kTasks][8];
+    load_a<FWD>(p, m, nv, t, f0, 0, va);
     for (int c = 0; c < nchunks; ++c) {
         const int s = c & 1;
         uint8_t* st = smem + s * stage_bytes;
@@ -557,7 +743,8 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
         }
         __syncthreads();
         if (s_abort) break;
-        produce_a<FWD>(p, st, m, nv, t, f0, c);
+        store_a(st, va);
+        if (c + 1 < nchunks) load_a<FWD>(p, m, nv, t, f0, c + 1, va);  // in flight across the MMA issue
         tc::fence_proxy_async_smem();
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -584,56 +771,53 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
         if (!tc::mbar_wait(&bars[2 + (last & 1)], (last >> 1) & 1)) s_abort = 1;
     }
     __syncthreads();
+    // Epilogue: TMEM -> registers (warps 0-3, one accumulator row per thread) -> padded smem
+    // tile D[r][i] (stage buffers are free once the last commit has arrived) -> all 8 warps
+    // write the outputs with consecutive threads on consecutive columns.
+    float* dt = reinterpret_cast<float*>(smem);
+    const int DS = NP + 1;  // odd row stride
     if (!s_abort && warp < 4) {
         tc::tc_fence_after();
         const int r = warp * 32 + lane;
-        const int f = f0 + (r & 63), part = r >> 6;
-        const bool live = f < p.N;
         const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int cb = 0; cb < NP; cb += 16) {
+            float v[16];
+            ld_sum(trow + cb, NP, p.nprod > 1, v);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) dt[r * DS + cb + q] = v[q];
+        }
+    }
+    __syncthreads();
+    if (!s_abort) {
         if (FWD) {
-            float* out = (part ? p.ic : p.rc) + (size_t)f * B * B;
             const int base = index_of_harmonic_coeff(m, m, B) + t;
             const int nbase = index_of_harmonic_coeff(-m, m, B) + t;
-            const float sneg = ((m & 1) ? -1.f : 1.f) * (part ? -1.f : 1.f);
-            const int lim = B - m - t;  // valid 2i
-            for (int cb = 0; cb < NP; cb += 16) {
-                float v[16];
-                ld_sum(trow + cb, NP, p.nprod > 1, v);
-                if (live) {
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const int d = 2 * (cb + q);
-                        if (d < lim) {
-                            out[base + d] = v[q];
-                            if (m) out[nbase + d] = sneg * v[q];
-                        }
-                    }
-                }
+            const int nv_ = (B - m - t + 1) / 2;  // degrees of this parity
+            for (int e = threadIdx.x; e < 128 * nv_; e += kTPB) {
+                const int r = e / nv_, i = e - r * nv_;
+                const int f = f0 + (r & 63), part = r >> 6;
+                if (f >= p.N) continue;
+                const float v = dt[r * DS + i];
+                float* out = (part ? p.ic : p.rc) + (size_t)f * B * B;
+                out[base + 2 * i] = v;
+                if (m) out[nbase + 2 * i] = (((m & 1) ? -1.f : 1.f) * (part ? -1.f : 1.f)) * v;
             }
         } else if (!nv) {
-            float* out = p.Fc + (((size_t)part * p.N + f) * B + m) * B + t;
             const float sc = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
-            for (int cb = 0; cb < NP; cb += 16) {
-                float v[16];
-                ld_sum(trow + cb, NP, p.nprod > 1, v);
-                if (live) {
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const int k = 2 * (cb + q);
-                        if (k < B) out[k] = v[q] * ((k + t == 0) ? sc0 : sc);
-                    }
-                }
+            const int nj = B / 2;
+            for (int e = threadIdx.x; e < 128 * nj; e += kTPB) {
+                const int r = e / nj, j = e - r * nj;
+                const int f = f0 + (r & 63), part = r >> 6;
+                if (f >= p.N) continue;
+                const int k = 2 * j + t;
+                p.Fc[(((size_t)part * p.N + f) * B + m) * B + k] = dt[r * DS + j] * (k == 0 ? sc0 : sc);
             }
         } else {
-            float* out = p.F + (((size_t)part * p.N + f) * B + m) * (2 * B) + t * B + nb * NP;
-            for (int cb = 0; cb < NP; cb += 16) {
-                float v[16];
-                ld_sum(trow + cb, NP, p.nprod > 1, v);
-                if (live) {
-#pragma unroll
-                    for (int q = 0; q < 16; q += 4)
-                        *reinterpret_cast<float4*>(out + cb + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
-                }
+            for (int e = threadIdx.x; e < 128 * NP; e += kTPB) {
+                const int r = e / NP, i = e - r * NP;
+                const int f = f0 + (r & 63), part = r >> 6;
+                if (f >= p.N) continue;
+                p.F[(((size_t)part * p.N + f) * B + m) * (2 * B) + t * B + nb * NP + i] = dt[r * DS + i];
             }
         }
     }
@@ -650,11 +834,6 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
 size_t split_work_bytes(int bw, int batch) {
     const size_t B = bw, S = 2 * B;
     return 2 * (size_t)batch * B * (S + B) * sizeof(float) + 1024;
-}
-
-static int dct_rows_per_cta(int S) {
-    int R = 8192 / S;
-    return R < 1 ? 1 : (R > 32 ? 32 : R);
 }
 
 static int set_smem(const void* fn, size_t bytes) {
@@ -676,7 +855,7 @@ static int launch_leg(bool fwd, Leg& p, cudaStream_t st) {
     S2G_TRY(set_smem(fn, smem));
     int nblk = 1;
     for (int m = 0; m < p.B; ++m) nblk = std::max(nblk, geo(fwd, p.B, m).nblk);
-    dim3 grid(p.B, (p.N + 63) / 64, 2 * nblk);
+    dim3 grid(2 * nblk, p.B, (p.N + 63) / 64);
     if (fwd)
         {
             ProfScope ps_("leg_tc_fwd", st);
@@ -691,7 +870,55 @@ static int launch_leg(bool fwd, Leg& p, cudaStream_t st) {
     return S2G_OK;
 }
 
-static int rows_r(int S) { return (4096 / S) < 1 ? 1 : ((4096 / S) > 32 ? 32 : 4096 / S); }
+// ---- warp-FFT kernel launchers (dispatch on R = S / 32) ----
+template <int R>
+static int launch_fft_kernels(int which, const void* in, void* out, int N, const Split* s, cudaStream_t st,
+                              float scale) {
+    constexpr int S = 32 * R, B = S / 2;
+    constexpr int PS = S + S / 32;
+    const int nrows = N * B;
+    size_t smem = 0;
+    if (which == 0) {  // rows forward
+        smem = sizeof(float) * (2 * twtab_len(S) + 2 * kWarps * PS + 2 * kLatPerCta * (B + B / 32 + 1));
+        S2G_TRY(set_smem((const void*)k_rows_fwd_w<R>, smem));
+        dim3 g((S + kLatPerCta - 1) / kLatPerCta, N);
+        ProfScope ps_("rows_fwd_f32", st);
+        k_rows_fwd_w<R><<<g, 256, smem, st>>>((const float*)in, (float*)out, N, scale, s->twS);
+    } else if (which == 1) {  // DCT-II
+        smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + 2 * S + 2 * kWarps * PS);
+        S2G_TRY(set_smem((const void*)k_dct_fwd_w<R>, smem));
+        ProfScope ps_("dct_fwd_f32", st);
+        k_dct_fwd_w<R><<<(nrows + kWarps - 1) / kWarps, 256, smem, st>>>((const float*)in, (float*)out, nrows, s->w32,
+                                                                        s->twS, s->twD);
+    } else if (which == 2) {  // DCT-III
+        smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + S + 2 * kWarps * PS);
+        S2G_TRY(set_smem((const void*)k_dct_inv_w<R>, smem));
+        ProfScope ps_("dct_inv_f32", st);
+        k_dct_inv_w<R><<<(nrows + kWarps - 1) / kWarps, 256, smem, st>>>((const float*)in, (float*)out, nrows,
+                                                                        s->sin32, s->twS, s->twD, scale);
+    } else {  // rows inverse
+        smem = sizeof(float) * (2 * twtab_len(S) + 2 * B * (kLatPerCta + 1) + 2 * kWarps * PS);
+        S2G_TRY(set_smem((const void*)k_rows_inv_w<R>, smem));
+        dim3 g((S + kLatPerCta - 1) / kLatPerCta, N);
+        ProfScope ps_("rows_inv_f32", st);
+        k_rows_inv_w<R><<<g, 256, smem, st>>>((const float*)in, (float*)out, N, s->twS);
+    }
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+static int fft_kernels(int which, int B, const void* in, void* out, int N, const Split* s, cudaStream_t st,
+                       float scale) {
+    switch (2 * B / 32) {
+        case 1: return launch_fft_kernels<1>(which, in, out, N, s, st, scale);
+        case 2: return launch_fft_kernels<2>(which, in, out, N, s, st, scale);
+        case 4: return launch_fft_kernels<4>(which, in, out, N, s, st, scale);
+        case 8: return launch_fft_kernels<8>(which, in, out, N, s, st, scale);
+        case 16: return launch_fft_kernels<16>(which, in, out, N, s, st, scale);
+        case 32: return launch_fft_kernels<32>(which, in, out, N, s, st, scale);
+        default: return fail(S2G_ERR_UNSUPPORTED, "no warp FFT for bandwidth %d", B);
+    }
+}
 
 int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int precision, void* work,
               cudaStream_t st) {
@@ -700,34 +927,12 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
     S2G_TRY(build_split(t));
     Split* s = (Split*)t->split;
     const int B = t->bw, S = 2 * B;
-    const Len L = make_len(S);
     float* X = (float*)work;
     float* Cb = X + 2 * (size_t)batch * B * S;
-    // 1. DFT along phi (two real latitudes per complex DFT), scaled by sqrt(2 pi)/S
-    {
-        const int R = rows_r(S);
-        const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
-        S2G_TRY(set_smem((const void*)k_rows_fwd<float, float2>, smem));
-        dim3 grid2((S + 2 * R - 1) / (2 * R), batch);
-        {
-            ProfScope ps_("rows_fwd_f32", st);
-            k_rows_fwd<float, float2><<<grid2, 256, smem, st>>>(grid, nullptr, X, X + (size_t)batch * B * S, S, L.logn, B,
-                                                               R, (float)(sqrt(2.0 * kPi) / S), s->twS);
-        }
-        S2G_CUDA(cudaGetLastError());
-    }
-    // 2. weighted DCT-II per (function, seminaive order)
-    {
-        const int nrows = batch * B;
-        const int R = dct_rows_per_cta(S);
-        const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
-        S2G_TRY(set_smem((const void*)k_dct_fwd32, smem));
-        {
-            ProfScope ps_("dct_fwd_f32", st);
-            k_dct_fwd32<<<(nrows + R - 1) / R, 256, smem, st>>>(X, Cb, nrows, B, L.logn, R, s->w32, s->twS, s->twD);
-        }
-        S2G_CUDA(cudaGetLastError());
-    }
+    // 1. DFT along phi (two real latitudes per warp), scaled by sqrt(2 pi)/S   (FST_semi_memo.c:81-90)
+    S2G_TRY(fft_kernels(0, B, grid, X, batch, s, st, (float)(sqrt(2.0 * kPi) / S)));
+    // 2. weighted DCT-II per (function, seminaive order)                      (seminaive.c:161-176)
+    S2G_TRY(fft_kernels(1, B, X, Cb, batch, s, st, 1.f));
     // 3. tensor-core contraction (seminaive orders from C, naive orders from X)
     Leg p{};
     p.C = Cb;
@@ -750,7 +955,6 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
     S2G_TRY(build_split(t));
     Split* s = (Split*)t->split;
     const int B = t->bw, S = 2 * B;
-    const Len L = make_len(S);
     float* F = (float*)work;
     float* Fc = F + 2 * (size_t)batch * B * S;
     const float scale = (float)(1.0 / sqrt(2.0 * kPi));
@@ -766,37 +970,16 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
     p.N = batch;
     p.nprod = nprod;
     S2G_TRY(launch_leg(false, p, st));
+    // REDFT01 (+ sin(theta) for odd m), scaled by 1/sqrt(2 pi)              (seminaive.c:105-114)
+    S2G_TRY(fft_kernels(2, B, Fc, F, batch, s, st, scale));
     {
-        const int nrows = batch * B;
-        const int R = dct_rows_per_cta(S);
-        const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
-        S2G_TRY(set_smem((const void*)k_dct_inv32, smem));
-        {
-            ProfScope ps_("dct_inv_f32", st);
-            k_dct_inv32<<<(nrows + R - 1) / R, 256, smem, st>>>(Fc, F, nrows, B, L.logn, R, s->sin32, s->twS, s->twD,
-                                                                 scale);
-        }
-        S2G_CUDA(cudaGetLastError());
         const int nnaive = std::min(B, kNaiveOddBelow) / 2;
-        {
-            ProfScope ps_("naive_combine_f32", st);
-            k_naive_combine<<<dim3(batch * nnaive, 2), 256, S * sizeof(float), st>>>(F, batch, B, scale);
-        }
+        ProfScope ps_("naive_combine_f32", st);
+        k_naive_combine<<<dim3(batch * nnaive, 2), 256, S * sizeof(float), st>>>(F, batch, B, scale);
         S2G_CUDA(cudaGetLastError());
     }
-    {
-        const int R = rows_r(S);
-        const size_t smem = (size_t)2 * R * (S + 1) * sizeof(float);
-        S2G_TRY(set_smem((const void*)k_rows_inv<float, float2>, smem));
-        dim3 grid2((S + 2 * R - 1) / (2 * R), batch);
-        {
-            ProfScope ps_("k_rows_inv<float, float2>", st);
-            k_rows_inv<float, float2><<<grid2, 256, smem, st>>>(F, F + (size_t)batch * B * S, B, 0, grid, nullptr, S,
-                                                               L.logn, R, s->twS);
-        }
-        S2G_CUDA(cudaGetLastError());
-    }
-    return S2G_OK;
+    // DFT with sign +1 over the orders, Hermitian rows                      (FST_semi_memo.c:334-350)
+    return fft_kernels(3, B, F, grid, batch, s, st, 1.f);
 }
 
 int split_device_status(Tables* t, int clear) {
