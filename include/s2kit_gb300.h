@@ -179,6 +179,20 @@ int s2g_fst_real_f32(s2g_plan plan, const float* grid, float* rcoeffs, float* ic
 int s2g_inv_fst_real_f32(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid, int batch,
                          int precision, void* stream);
 
+/* Forward FP64 transform of ONE function that allocates no device memory (no counterpart in
+ * the reference).  For callers that cannot call cudaMalloc/cudaFree -- code running inside a
+ * framework that has already reserved its device memory budget, or latency-critical code that
+ * cannot accept the implicit synchronisation of allocation -- the intermediate buffer and the
+ * twiddle factors live in a fixed __device__ array of about 4 MiB held by every GPU that loads
+ * the library.  All pointers are device pointers: samples, coefficients (as s2g_fst), the
+ * seminaive/naive table in the SemiNaive_Naive_Pml_Table layout with its bw int64 order offsets,
+ * and the 4*bw quadrature weights.  bw <= 256; larger bw is rejected with S2G_ERR_ARG.  The first
+ * call on a device looks up the array's device address (make that first call before any stream
+ * capture).  Calls share the array, so calls that overlap on the GPU race: serialise them. */
+int s2g_fst_noalloc(const double* rdata, const double* idata, double* rcoeffs, double* icoeffs, int bw,
+                    const double* table, const int64_t* table_offsets, const double* weights,
+                    DataFormat data_format, int cutoff, void* stream);
+
 /* Same on HOST buffers: copies in, transforms, copies out (chunked, copies overlapped with
  * compute on the plan's streams); returns when the results are in host memory. */
 int s2g_fst_real_f32_host(s2g_plan plan, const float* grid, float* rcoeffs, float* icoeffs, int batch,

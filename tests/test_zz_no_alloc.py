@@ -1,0 +1,74 @@
+"""The forward transform entry point that allocates no device memory (s2g_fst_noalloc).
+
+It serves callers that cannot call cudaMalloc/cudaFree (code inside a framework that has
+already reserved its device memory, or code that cannot accept the synchronisation an
+allocation implies): its scratch is a fixed __device__ array.  The test calls it through the
+C ABI twice in a row, with different inputs, and checks each result against the existing
+batched entry point s2g_fst on the same inputs, with the FP64 tolerance of the other tests.
+This file is collected last so that a failure here never hides the rest of the suite.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import s2kit_gb300 as s2
+from s2kit_gb300 import api
+from tests._util import rel_err_norm
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-11
+
+
+def _device_tables(torch, bw, cutoff):
+    size = api.Reduced_Naive_TableSize(bw, cutoff) + api.Reduced_SpharmonicTableSize(bw, cutoff)
+    space = np.zeros(size)
+    api.SemiNaive_Naive_Pml_Table(bw, cutoff, space, None)
+    off = np.zeros(bw, dtype=np.int64)
+    o = 0
+    for m in range(bw):
+        off[m] = o
+        o += api.TableSize(m, bw) if m < cutoff else 2 * bw * (bw - m)
+    w = np.zeros(4 * bw)
+    api.GenerateWeightsForDLT(bw, w)
+    return torch.from_numpy(space).cuda(), torch.from_numpy(off).cuda(), torch.from_numpy(w).cuda()
+
+
+def _call(lib, rd, idd, rc, ic, bw, tab, off, w, fmt, cutoff):
+    st = lib.s2g_fst_noalloc(rd.data_ptr(), idd.data_ptr() if idd is not None else None, rc.data_ptr(),
+                             ic.data_ptr(), bw, tab.data_ptr(), off.data_ptr(), w.data_ptr(), fmt, cutoff, None)
+    assert st == 0, lib.s2g_last_error()
+
+
+@pytest.mark.parametrize("bw,cutoff", [(64, 64), (256, 256), (32, 8)])
+def test_noalloc_matches_fst_twice(bw, cutoff):
+    import torch
+    lib = s2.load()
+    tab, off, w = _device_tables(torch, bw, cutoff)
+    plan = api.Plan(bw, cutoff)
+    rng = np.random.default_rng(bw + cutoff)
+    n = 2 * bw
+    for call, fmt in enumerate((api.REAL, api.COMPLEX)):
+        rd = torch.from_numpy(rng.standard_normal(n * n)).cuda()
+        idd = torch.from_numpy(rng.standard_normal(n * n)).cuda()
+        rc = torch.full((bw * bw,), float("nan"), dtype=torch.float64, device="cuda")
+        ic = torch.full_like(rc, float("nan"))
+        _call(lib, rd, idd, rc, ic, bw, tab, off, w, fmt, cutoff)
+        ref_r = torch.zeros_like(rc)
+        ref_i = torch.zeros_like(rc)
+        plan.fst(rd, idd, ref_r, ref_i, 1, fmt)
+        torch.cuda.synchronize()
+        assert torch.isfinite(rc).all() and torch.isfinite(ic).all(), f"call {call}"
+        err = rel_err_norm(rc.cpu().numpy(), ic.cpu().numpy(), ref_r.cpu().numpy(), ref_i.cpu().numpy())
+        assert err <= TOL, (call, err)
+
+
+def test_noalloc_rejects_bandwidth_beyond_scratch():
+    import torch
+    lib = s2.load()
+    x = torch.zeros(16, dtype=torch.float64, device="cuda")
+    off = torch.zeros(16, dtype=torch.int64, device="cuda")
+    st = lib.s2g_fst_noalloc(x.data_ptr(), x.data_ptr(), x.data_ptr(), x.data_ptr(), 512, x.data_ptr(),
+                             off.data_ptr(), x.data_ptr(), api.REAL, 512, None)
+    assert st == 1
+    assert b"bandwidth 512" in lib.s2g_last_error()
