@@ -76,6 +76,21 @@ def real_field_coeffs(rng, bw, p, nfunc):
     return rc, ic
 
 
+def reduce_max(x, dist, device):
+    """Max of a per-rank scalar over all ranks (the timing rule: the slowest rank sets the step)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
+def weak_scaling_value(n_per_rank, world_size, ms_max):
+    """Whole-job throughput: every rank transforms its own batch; the job takes the slowest rank's time."""
+    return world_size * n_per_rank / (ms_max / 1e3)
+
+
 def config(args):
     return {
         "workload": f"real-field SHT fwd+inv, bandwidth {args.bw} ({2 * args.bw}x{2 * args.bw} Driscoll-Healy grid), "
@@ -266,12 +281,8 @@ def main():
     torch.cuda.synchronize()
     barrier()
     launches = lib.s2g_launch_count() - launches0
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
-    value = ws * N / (ms / 1e3)
+    ms = reduce_max(e0.elapsed_time(e1) / args.steps, dist, "cuda")
+    value = weak_scaling_value(N, ws, ms)
     plan.sync_status()
 
     # ---- per-kernel event timing pass (same steps, every launch bracketed by events)
@@ -361,12 +372,8 @@ def main():
     for _ in range(ke):
         step_e2e()
     t1 = time.perf_counter()
-    ms_e2e = 1e3 * (t1 - t0) / ke
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = t.item()
-    e2e_value = ws * N / (ms_e2e / 1e3)
+    ms_e2e = reduce_max(1e3 * (t1 - t0) / ke, dist, "cuda")
+    e2e_value = weak_scaling_value(N, ws, ms_e2e)
     h2d = h_rc.nbytes + h_ic.nbytes + h_grid.nbytes
     d2h = h_grid.nbytes + h_orc.nbytes + h_oic.nbytes
     clk = clocks.stop()
@@ -409,7 +416,6 @@ def main():
 
 def tc_flops_issued(B, N, fwd, nprod):
     """MMA flops issued by one launch (dense padded tiles, all split products)."""
-    nn = min(B, 32) // 2
     tot = 0
     for m in range(B):
         naive = (m & 1) and m < 32
@@ -423,19 +429,14 @@ def tc_flops_issued(B, N, fwd, nprod):
             n_ = (min(B, 256) if naive else B // 2) * (B // min(B, 256) if naive else 1)
         kpad = ((kx + 31) // 32) * 32
         tot += 2 * 128 * n_ * kpad * 2 * nprod  # both parities, M = 128 rows
-    tiles = (N + 63) // 64
-    _ = nn
-    return tot * tiles
+    return tot * ((N + 63) // 64)
 
 
 def useful_flops(B, N):
     """Seminaive Legendre flops of one direction: 4 * table entries per function (re + im)."""
     table = 0
-    for m in range(B):
-        k = m // 2
-        # sum_{l=m}^{B-1} RowSize(m, l)
+    for m in range(B):  # sum over l = m..B-1 of RowSize(m, l)
         table += sum((l // 2 + 1) if m % 2 == 0 else ((l - 1) // 2 + 1) for l in range(m, B))
-        _ = k
     return 4 * table * N
 
 

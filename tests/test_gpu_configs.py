@@ -1,0 +1,79 @@
+"""BASELINE configurations 3 and 5 on the GPU (configs 1 and 2 are in test_gpu_fp64.py).
+
+Config 3: 4096 real functions at bw 64 in one launch, FP32 samples, coefficients
+N(0,1)(1+l)^-1.5, 3-term split BF16 contraction: error vs the FP64 path <= 1e-6 (normwise).
+Config 5 (FP64 part): 2 real functions at bw 1024, coefficients N(0,1)(1+l)^-1: inverse then
+forward recovers the coefficients to 1e-10; the convolution with the zonal filter
+h_l^0 = exp(-l(l+1)/(2*150^2)) satisfies the convolution theorem: FST(conv) equals TransMult of
+FST(data) and FZT(filter).
+"""
+import numpy as np
+import pytest
+
+from s2kit_gb300 import api
+from tests._util import harmonic_index, real_field_coeffs
+
+pytestmark = pytest.mark.gpu
+
+
+def test_config3_batched_uniform_bw64():
+    import torch
+    bw, nb = 64, 4096
+    rng = np.random.default_rng(3)
+    rc, ic = real_field_coeffs(rng, bw, 1.5, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    g64 = torch.empty(nb, 4 * bw * bw, dtype=torch.float64, device="cuda")
+    plan.inv_fst(d_rc, d_ic, g64, None, nb, api.REAL)
+    f_rc, f_ic = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    plan.fst(g64, None, f_rc, f_ic, nb, api.REAL)
+    s_rc = torch.empty(nb, bw * bw, dtype=torch.float32, device="cuda")
+    s_ic = torch.empty_like(s_rc)
+    plan.fst_real_f32(g64.float(), s_rc, s_ic, nb, api.PREC_BF16X3)
+    s_g = torch.empty(nb, 4 * bw * bw, dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(d_rc.float(), d_ic.float(), s_g, nb, api.PREC_BF16X3)
+    plan.sync_status()
+    mag = torch.hypot(f_rc, f_ic).amax(1)
+    e_fwd = (torch.hypot(s_rc.double() - f_rc, s_ic.double() - f_ic).amax(1) / mag).max().item()
+    e_inv = ((s_g.double() - g64).abs().amax(1) / g64.abs().amax(1)).max().item()
+    assert e_fwd <= 1e-6 and e_inv <= 1e-6, (e_fwd, e_inv)
+
+
+def test_config5_fp64_bw1024_roundtrip_and_conv():
+    import torch
+    bw, nb = 1024, 2
+    rng = np.random.default_rng(5)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    grid = torch.empty(nb, 4 * bw * bw, dtype=torch.float64, device="cuda")
+    plan.inv_fst(d_rc, d_ic, grid, None, nb, api.REAL)
+    o_rc, o_ic = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    plan.fst(grid, None, o_rc, o_ic, nb, api.REAL)
+    torch.cuda.synchronize()
+    mag = torch.hypot(d_rc, d_ic).amax(1)
+    e = (torch.hypot(o_rc - d_rc, o_ic - d_ic).amax(1) / mag).max().item()
+    assert e <= 1e-10, e
+    # zonal filter grid, convolution, and the convolution theorem in coefficient space
+    l = np.arange(bw)
+    hr = np.zeros((nb, bw * bw))
+    hr[:, harmonic_index(0, l, bw)] = np.exp(-l * (l + 1) / (2 * 150.0 ** 2))
+    d_hr = torch.from_numpy(hr).cuda()
+    z = torch.zeros_like(d_hr)
+    fgrid = torch.empty_like(grid)
+    plan.inv_fst(d_hr, z, fgrid, None, nb, api.REAL)
+    zero = torch.zeros_like(grid)
+    cr, ci = torch.empty_like(grid), torch.empty_like(grid)
+    plan.conv(grid, zero, fgrid, zero, cr, ci, nb)
+    c_rc, c_ic = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    plan.fst(cr, None, c_rc, c_ic, nb, api.REAL)
+    zr, zi = torch.empty(nb, bw, dtype=torch.float64, device="cuda"), torch.empty(nb, bw, dtype=torch.float64,
+                                                                                  device="cuda")
+    plan.fzt(fgrid, zero, zr, zi, nb, api.REAL)
+    tr, ti = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    api.transmult(bw, o_rc, o_ic, zr, zi, tr, ti, nb)
+    torch.cuda.synchronize()
+    scale = torch.hypot(tr, ti).amax(1)
+    e = (torch.hypot(c_rc - tr, c_ic - ti).amax(1) / scale).max().item()
+    assert e <= 1e-10, e
+    assert ci.abs().max().item() <= 1e-10 * cr.abs().max().item()
