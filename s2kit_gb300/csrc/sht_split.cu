@@ -729,18 +729,21 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
     const uint32_t idesc = tc::idesc_bf16_f32(128, NP);
     constexpr uint32_t sbo = (kKC / 8) * 128;
 
+    // Table chunks: 0 and 1 are issued here; chunk c+1 is issued right after the MMAs of chunk
+    // c, as soon as those of chunk c-1 (the previous user of that stage) have retired.
+    if (threadIdx.x == 0) {
+        for (int c = 0; c < 2 && c < nchunks; ++c) {
+            tc::mbar_arrive_expect_tx(&bars[c], 3 * bt);
+            tc::bulk_g2s(smem + c * stage_bytes + 3 * kATile, blob + (size_t)c * 3 * bt, 3 * bt, &bars[c]);
+        }
+    }
     float va[kTasks][8];
     load_a<FWD>(p, m, nv, t, f0, 0, va);
     for (int c = 0; c < nchunks; ++c) {
         const int s = c & 1;
         uint8_t* st = smem + s * stage_bytes;
-        if (threadIdx.x == 0) {
-            if (c >= 2 && !tc::mbar_wait(&bars[2 + s], ((c - 2) >> 1) & 1)) s_abort = 1;
-            if (!s_abort) {
-                tc::mbar_arrive_expect_tx(&bars[s], 3 * bt);
-                tc::bulk_g2s(st + 3 * kATile, blob + (size_t)c * 3 * bt, 3 * bt, &bars[s]);
-            }
-        }
+        // the A part of stage s was last read by the MMAs of chunk c-2; thread 0 waited for them
+        // at the end of iteration c-1, before it issued the table copy of chunk c into stage s
         __syncthreads();
         if (s_abort) break;
         store_a(st, va);
@@ -762,6 +765,16 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
                     }
                 }
                 tc::mma_commit(&bars[2 + s]);
+                // stage s^1 is free once the MMAs of chunk c-1 retire: fetch chunk c+1 into it
+                if (c + 1 < nchunks && c >= 1) {
+                    if (!tc::mbar_wait(&bars[2 + (s ^ 1)], ((c - 1) >> 1) & 1)) {
+                        s_abort = 1;
+                    } else {
+                        uint8_t* sn = smem + (s ^ 1) * stage_bytes;
+                        tc::mbar_arrive_expect_tx(&bars[s ^ 1], 3 * bt);
+                        tc::bulk_g2s(sn + 3 * kATile, blob + (size_t)(c + 1) * 3 * bt, 3 * bt, &bars[s ^ 1]);
+                    }
+                }
             }
         }
     }
