@@ -126,7 +126,8 @@ typedef enum {
 typedef enum {
     S2G_PREC_FP64 = 0,   /* plain FP64 everywhere (parity path) */
     S2G_PREC_BF16X3 = 1, /* FP32 FFT/DCT, Legendre contraction as 3-term split BF16 on tcgen05, FP32 accumulate */
-    S2G_PREC_BF16X2 = 2  /* as above with 2-term splits (3 products) */
+    S2G_PREC_BF16X2 = 2, /* as above with 2-term splits (3 products) */
+    S2G_PREC_FP16X2 = 3  /* 2-term split FP16 (3 products), rows and table scaled by powers of two */
 } s2g_precision;
 
 /* Last error message of the calling thread ("" if none). */
@@ -170,7 +171,7 @@ int s2g_conv(s2g_plan plan, const double* rdata, const double* idata, const doub
              const double* ifilter, double* rres, double* ires, int batch, void* stream);
 
 /* Real-field batched transforms with FP32 samples/coefficients and a selectable
- * precision for the Legendre contraction (s2g_precision); power-of-two bw in [16, 512],
+ * precision for the Legendre contraction (s2g_precision); power-of-two bw in [16, 1024],
  * plan cutoff == bw.  grid: batch*(2bw)^2 floats;
  * rcoeffs/icoeffs: batch*bw*bw floats in the reference layout, negative orders filled by
  * f(l,-m) = (-1)^m conj f(l,m) on output and ignored on input. */
@@ -178,6 +179,18 @@ int s2g_fst_real_f32(s2g_plan plan, const float* grid, float* rcoeffs, float* ic
                      void* stream);
 int s2g_inv_fst_real_f32(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid, int batch,
                          int precision, void* stream);
+
+/* Real-field transforms with FP64 samples and coefficients whose Legendre contraction runs as
+ * split products (precision: S2G_PREC_BF16X3, _BF16X2 or _FP16X2) followed by one refinement
+ * step with an FP64 residual: forward a1 = F(f), a = a1 + F(f - I64(a1)); inverse g1 = I(a),
+ * g = g1 + I(a - F64(g1)), where I64/F64 are the FP64 transforms on the GPU.  The error falls
+ * from about e (the split path's) to about e^2 (below 1e-10 with BF16X3).  Layouts as
+ * s2g_fst_real_f32 (the inverse reads the non-negative orders); power-of-two bw in [16, 1024],
+ * plan cutoff == bw.  The plan grows its own scratch. */
+int s2g_fst_refined(s2g_plan plan, const double* grid, double* rcoeffs, double* icoeffs, int batch, int precision,
+                    void* stream);
+int s2g_inv_fst_refined(s2g_plan plan, const double* rcoeffs, const double* icoeffs, double* grid, int batch,
+                        int precision, void* stream);
 
 /* Forward FP64 transform of ONE function that allocates no device memory (no counterpart in
  * the reference).  For callers that cannot call cudaMalloc/cudaFree -- code running inside a
@@ -204,12 +217,52 @@ int s2g_inv_fst_real_f32_host(s2g_plan plan, const float* rcoeffs, const float* 
  * tensor-core kernels (S2G_ERR_TIMEOUT when a bounded wait expired); clears the record. */
 int s2g_plan_sync_status(s2g_plan plan);
 
+/* Grouped transforms of many real functions of uneven bandwidth (no counterpart in the
+ * reference, which transforms one function per call).  Function f has bandwidth bw[f], a power
+ * of two in [16, 512]; precision is a split mode (S2G_PREC_BF16X3, _BF16X2 or _FP16X2).  Layout
+ * on the device: the functions back to back in the order given, function f's grid taking
+ * (2 bw[f])^2 floats and its coefficients bw[f]^2 floats in each of rcoeffs/icoeffs (the
+ * reference layout per function, negative orders written by symmetry as s2g_fst_real_f32);
+ * s2g_group_layout returns the offsets.  A call runs the phi-FFT/DCT stages of each bandwidth
+ * class concurrently and ONE persistent tensor-core contraction launch over all classes; the
+ * sequence is captured as a CUDA graph on the first call with a given set of pointers and
+ * replayed on later calls with the same pointers.  Calls on one group must be serialised (they
+ * share the group's intermediate buffers). */
+typedef struct s2g_group_s* s2g_group;
+int s2g_group_create(s2g_group* group, int nfunc, const int* bw, int precision);
+int s2g_group_destroy(s2g_group group);
+int s2g_group_layout(s2g_group group, int64_t* grid_offsets, int64_t* coeff_offsets, int64_t* grid_total,
+                     int64_t* coeff_total);
+int s2g_group_fst(s2g_group group, const float* grid, float* rcoeffs, float* icoeffs, void* stream);
+int s2g_group_inv_fst(s2g_group group, const float* rcoeffs, const float* icoeffs, float* grid, void* stream);
+/* forward of grid into the coefficients, then inverse of those into grid_out, one graph */
+int s2g_group_fst_inv(s2g_group group, const float* grid, float* rcoeffs, float* icoeffs, float* grid_out,
+                      void* stream);
+/* Times candidate tile shapes (N extent of each class's contraction tile, CTAs per SM of the
+ * persistent kernel) on the group's sizes and keeps the fastest.  Results are cached per
+ * (device, precision, class sizes); force != 0 re-measures.  $S2G_TUNE_CACHE, when set, names a
+ * file that keeps them across processes.  Synchronous. */
+int s2g_group_autotune(s2g_group group, int force);
+/* Sets the shapes by hand: ctas_per_sm (0 = as many as fit) and one tile N per bandwidth class
+ * in increasing bandwidth (0 = the class's whole table-row extent; NULL = all 0). */
+int s2g_group_set_tiles(s2g_group group, int ctas_per_sm, const int* tile_n);
+/* JSON description: classes [bw, count], chosen tiles, kernels per captured graph. */
+int s2g_group_describe(s2g_group group, char* buf, size_t len);
+/* Waits for the device and reports a failure recorded by the tensor-core kernels. */
+int s2g_group_sync_status(s2g_group group);
+
 /* ========================== Part 3: diagnostics =================================== */
 
 /* Runs the split-BF16 tcgen05 machinery on one tile: D[128 x N] = A[128 x K] * B[N x K]^T
  * (row-major FP32 device arrays, N and K multiples of 16, N <= 256, K <= 128) with `nprod`
  * of the six split products (1 = plain BF16 ... 6 = 3-term split).  Synchronous. */
 int s2g_selftest_tc(int N, int K, int nprod, const float* A, const float* B, float* D);
+
+/* Selects the tensor-core contraction kernel for later calls (process-wide): 1 (default) =
+ * warp-specialised persistent kernel (scheduler/table-copy warp, MMA warp, A-producer warps,
+ * epilogue warps; one CTA per SM), 0 = the kernel in which all threads stage each chunk (two
+ * CTAs per SM).  Both do the same arithmetic per work item and give identical results. */
+int s2g_set_contraction_kernel(int which);
 
 /* Kernel timing: while enabled, every kernel the library launches is bracketed by CUDA
  * events on the stream it is launched on.  s2g_prof_enable() also discards earlier records.

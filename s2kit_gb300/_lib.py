@@ -63,7 +63,21 @@ SIGNATURES = {
     "s2g_fst_real_f32_host": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
     "s2g_inv_fst_real_f32_host": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
     "s2g_plan_sync_status": (C.c_int, [vp]),
+    "s2g_fst_refined": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, vp]),
+    "s2g_inv_fst_refined": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, vp]),
     "s2g_fst_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int, vp, vp, vp, C.c_int, C.c_int, vp]),
+    "s2g_group_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(C.c_int), C.c_int]),
+    "s2g_group_destroy": (C.c_int, [vp]),
+    "s2g_group_layout": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_int64)]),
+    "s2g_group_fst": (C.c_int, [vp, vp, vp, vp, vp]),
+    "s2g_group_inv_fst": (C.c_int, [vp, vp, vp, vp, vp]),
+    "s2g_group_fst_inv": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+    "s2g_group_autotune": (C.c_int, [vp, C.c_int]),
+    "s2g_group_set_tiles": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
+    "s2g_group_describe": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
+    "s2g_group_sync_status": (C.c_int, [vp]),
+    "s2g_set_contraction_kernel": (C.c_int, [C.c_int]),
     "s2g_selftest_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, vp]),
     "s2g_prof_enable": (C.c_int, [C.c_int]),
     "s2g_prof_report": (C.c_int, [C.c_char_p, C.c_size_t]),

@@ -15,7 +15,7 @@ import numpy as np
 from ._lib import check, dp, dpp, load
 
 COMPLEX, REAL = 0, 1
-PREC_FP64, PREC_BF16X3, PREC_BF16X2 = 0, 1, 2
+PREC_FP64, PREC_BF16X3, PREC_BF16X2, PREC_FP16X2 = 0, 1, 2, 3
 
 
 def _p(a):
@@ -218,6 +218,15 @@ class Plan:
         check(self.lib.s2g_inv_fst_real_f32(self.h, _addr(rcoeffs), _addr(icoeffs), _addr(grid), batch, precision,
                                             _stream(stream)), "s2g_inv_fst_real_f32")
 
+    def fst_refined(self, grid, rcoeffs, icoeffs, batch, precision=PREC_BF16X3, stream=None):
+        """FP64 in/out forward: split contraction plus one FP64-residual refinement step."""
+        check(self.lib.s2g_fst_refined(self.h, _addr(grid), _addr(rcoeffs), _addr(icoeffs), batch, precision,
+                                       _stream(stream)), "s2g_fst_refined")
+
+    def inv_fst_refined(self, rcoeffs, icoeffs, grid, batch, precision=PREC_BF16X3, stream=None):
+        check(self.lib.s2g_inv_fst_refined(self.h, _addr(rcoeffs), _addr(icoeffs), _addr(grid), batch, precision,
+                                           _stream(stream)), "s2g_inv_fst_refined")
+
     def fst_real_f32_host(self, grid: np.ndarray, rcoeffs: np.ndarray, icoeffs: np.ndarray, batch, precision):
         check(self.lib.s2g_fst_real_f32_host(self.h, grid.ctypes.data, rcoeffs.ctypes.data, icoeffs.ctypes.data,
                                              batch, precision), "s2g_fst_real_f32_host")
@@ -225,6 +234,70 @@ class Plan:
     def inv_fst_real_f32_host(self, rcoeffs: np.ndarray, icoeffs: np.ndarray, grid: np.ndarray, batch, precision):
         check(self.lib.s2g_inv_fst_real_f32_host(self.h, rcoeffs.ctypes.data, icoeffs.ctypes.data, grid.ctypes.data,
                                                  batch, precision), "s2g_inv_fst_real_f32_host")
+
+
+class Group:
+    """Grouped transforms of many real functions of uneven bandwidth (s2g_group_*).
+
+    ``bws``: bandwidth of each function (powers of two in [16, 512]).  Device buffers are flat
+    float32 tensors: the grid holds the functions' (2 bw)^2 samples back to back, rcoeffs/icoeffs
+    their bw^2 coefficients; ``grid_offsets``/``coeff_offsets`` give each function's start.
+    """
+
+    def __init__(self, bws, precision=PREC_FP16X2):
+        self.lib = load()
+        self.bws = [int(b) for b in bws]
+        self.precision = precision
+        h = C.c_void_p()
+        arr = (C.c_int * len(self.bws))(*self.bws)
+        check(self.lib.s2g_group_create(C.byref(h), len(self.bws), arr, precision), "s2g_group_create")
+        self.h = h
+        n = len(self.bws)
+        go, co = (C.c_int64 * n)(), (C.c_int64 * n)()
+        gt, ct = C.c_int64(), C.c_int64()
+        check(self.lib.s2g_group_layout(self.h, go, co, C.byref(gt), C.byref(ct)), "s2g_group_layout")
+        self.grid_offsets = np.array(go[:], dtype=np.int64)
+        self.coeff_offsets = np.array(co[:], dtype=np.int64)
+        self.grid_total, self.coeff_total = gt.value, ct.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.s2g_group_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fst(self, grid, rcoeffs, icoeffs, stream=None):
+        check(self.lib.s2g_group_fst(self.h, _addr(grid), _addr(rcoeffs), _addr(icoeffs), _stream(stream)),
+              "s2g_group_fst")
+
+    def inv_fst(self, rcoeffs, icoeffs, grid, stream=None):
+        check(self.lib.s2g_group_inv_fst(self.h, _addr(rcoeffs), _addr(icoeffs), _addr(grid), _stream(stream)),
+              "s2g_group_inv_fst")
+
+    def fst_inv(self, grid, rcoeffs, icoeffs, grid_out, stream=None):
+        check(self.lib.s2g_group_fst_inv(self.h, _addr(grid), _addr(rcoeffs), _addr(icoeffs), _addr(grid_out),
+                                         _stream(stream)), "s2g_group_fst_inv")
+
+    def autotune(self, force=False):
+        check(self.lib.s2g_group_autotune(self.h, 1 if force else 0), "s2g_group_autotune")
+
+    def set_tiles(self, ctas_per_sm=0, tile_n=None):
+        arr = None if tile_n is None else (C.c_int * len(tile_n))(*tile_n)
+        check(self.lib.s2g_group_set_tiles(self.h, ctas_per_sm, arr), "s2g_group_set_tiles")
+
+    def describe(self) -> dict:
+        import json
+        buf = C.create_string_buffer(4096)
+        check(self.lib.s2g_group_describe(self.h, buf, len(buf)), "s2g_group_describe")
+        return json.loads(buf.value.decode())
+
+    def sync_status(self):
+        check(self.lib.s2g_group_sync_status(self.h), "group device status")
 
 
 def selftest_tc(A, B, D, nprod=6):

@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "libs2kit_gb300.so")
 BUILD_DIR = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "tables.cu", "sht_fp64.cu", "sht_split.cu", "noalloc.cu"]
+SOURCES = ["capi.cu", "tables.cu", "sht_fp64.cu", "sht_split.cu", "group.cu", "refine.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -31,9 +31,12 @@ int fail(int code, const char* fmt, ...) {
     return code;
 }
 
+// name of the kernel this thread launched last (for launch-error messages)
+static thread_local const char* t_kernel = "";
+
 int cuda_fail(cudaError_t e, const char* what) {
-    return fail(e == cudaErrorMemoryAllocation ? S2G_ERR_NOMEM : S2G_ERR_CUDA, "%s: %s", what,
-                cudaGetErrorString(e));
+    return fail(e == cudaErrorMemoryAllocation ? S2G_ERR_NOMEM : S2G_ERR_CUDA, "%s: %s (last kernel launched: %s)",
+                what, cudaGetErrorString(e), t_kernel);
 }
 
 // ---------------------------------------------------------------------------------
@@ -60,7 +63,29 @@ static cudaEvent_t prof_event() {
     return e;
 }
 
+// While this thread captures a graph, launches are counted into the graph instead of the
+// process total (each replay adds them) and are not bracketed by events.
+static thread_local bool t_capturing = false;
+static thread_local unsigned long long t_captured = 0;
+
+void capture_count_begin() {
+    t_capturing = true;
+    t_captured = 0;
+}
+
+unsigned long long capture_count_end() {
+    t_capturing = false;
+    return t_captured;
+}
+
+void launches_add(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 void prof_begin(const char* name, cudaStream_t st) {
+    t_kernel = name;
+    if (t_capturing) {
+        ++t_captured;
+        return;
+    }
     g_launches.fetch_add(1, std::memory_order_relaxed);
     if (!g_prof_on.load(std::memory_order_relaxed)) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -71,7 +96,7 @@ void prof_begin(const char* name, cudaStream_t st) {
 }
 
 void prof_end(cudaStream_t st) {
-    if (!g_prof_on.load(std::memory_order_relaxed) || t_prof_open.empty()) return;
+    if (t_capturing || !g_prof_on.load(std::memory_order_relaxed) || t_prof_open.empty()) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     const size_t i = t_prof_open.back();
     t_prof_open.pop_back();
@@ -141,6 +166,8 @@ static std::map<std::tuple<int, int, int>, Tables*> g_tables;
 
 static void free_tables(Tables* t);
 
+// Returns the tables with one reference taken for the caller (released with put_tables); the
+// cache holds its own reference, so s2g_cache_clear() never frees tables a plan still uses.
 int get_tables(int bw, int cutoff, Tables** out) {
     int dev;
     S2G_TRY(current_device(&dev));
@@ -148,6 +175,7 @@ int get_tables(int bw, int cutoff, Tables** out) {
     auto key = std::make_tuple(dev, bw, cutoff);
     auto it = g_tables.find(key);
     if (it != g_tables.end()) {
+        ++it->second->refs;
         *out = it->second;
         return S2G_OK;
     }
@@ -163,9 +191,16 @@ int get_tables(int bw, int cutoff, Tables** out) {
         free_tables(t);
         return r;
     }
+    t->refs = 2;  // the cache and the caller
     g_tables[key] = t;
     *out = t;
     return S2G_OK;
+}
+
+void put_tables(Tables* t) {
+    if (!t) return;
+    std::lock_guard<std::mutex> lk(g_tab_mu);
+    if (--t->refs == 0) free_tables(t);
 }
 
 void free_split(Tables* t);
@@ -271,6 +306,7 @@ static int do_fst(double* rdata, double* idata, double* rcoeffs, double* icoeffs
     S2G_TRY(dropin_device());
     Tables* base;
     S2G_TRY(get_tables(bw, cutoff, &base));
+    TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
     S2G_TRY(upload_table(base, table, 0, &view.fwd));
@@ -300,6 +336,7 @@ static int do_inv_fst(double* rcoeffs, double* icoeffs, double* rdata, double* i
     S2G_TRY(dropin_device());
     Tables* base;
     S2G_TRY(get_tables(bw, cutoff, &base));
+    TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
     S2G_TRY(upload_table(base, ttable, 1, &view.inv));
@@ -324,6 +361,7 @@ static int do_fzt(double* rdata, double* idata, double* rres, double* ires, int 
     S2G_TRY(dropin_device());
     Tables* base;
     S2G_TRY(get_tables(bw, bw, &base));
+    TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
     const size_t S = 2 * (size_t)bw, ng = S * S, nt = (size_t)table_size(0, bw);
@@ -376,6 +414,7 @@ static int do_conv(double* rdata, double* idata, double* rfilter, double* ifilte
     S2G_TRY(dropin_device());
     Tables* t;
     S2G_TRY(get_tables(bw, bw, &t));
+    TabRef tref_{t};
     const size_t S = 2 * (size_t)bw, ng = S * S;
     static thread_local DropinScratch io;
     S2G_TRY(io.s.ensure(6 * rnd(ng) + 256));
@@ -400,6 +439,7 @@ static int do_dlt(int kind, const double* in, int bw, int m, double* out, const 
     S2G_TRY(dropin_device());
     Tables* t;
     S2G_TRY(get_tables(bw, bw, &t));
+    TabRef tref_{t};
     const size_t S = 2 * (size_t)bw;
     const size_t nt = (kind <= 1) ? (size_t)table_size(m, bw) : S * (size_t)(bw - m);
     const size_t nin = (kind == 0 || kind == 2) ? S : (size_t)(bw - m);
@@ -700,7 +740,8 @@ const char* s2g_version(void) { return "s2kit_gb300 0.1 (sm_103a)"; }
 
 int s2g_cache_clear(void) {
     std::lock_guard<std::mutex> lk(g_tab_mu);
-    for (auto& kv : g_tables) free_tables(kv.second);
+    for (auto& kv : g_tables)
+        if (--kv.second->refs == 0) free_tables(kv.second);
     g_tables.clear();
     for (auto& kv : g_uploads) cudaFree(kv.second.d);
     g_uploads.clear();
@@ -725,6 +766,7 @@ int s2g_plan_create(s2g_plan* plan, int bw, int cutoff) {
     S2G_TRY(current_device(&dev));
     Tables* t;
     S2G_TRY(get_tables(bw, cutoff, &t));
+    TabRef tref_{t};
     s2g_plan p = new s2g_plan_s();
     p->bw = bw;
     p->cutoff = cutoff;
@@ -732,6 +774,7 @@ int s2g_plan_create(s2g_plan* plan, int bw, int cutoff) {
     p->t = t;
     for (auto& s : p->streams) S2G_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     for (auto& e : p->events) S2G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    tref_.t = nullptr;  // the plan keeps the reference
     *plan = p;
     return S2G_OK;
 }
@@ -746,6 +789,7 @@ int s2g_plan_destroy(s2g_plan p) {
     for (auto e : p->events) cudaEventDestroy(e);
     p->work.release();
     p->io.release();
+    put_tables(p->t);
     delete p;
     return S2G_OK;
 }
@@ -817,6 +861,24 @@ int s2g_inv_fst_real_f32(s2g_plan p, const float* rc, const float* ic, float* gr
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(p->work.ensure(split_work_bytes(p->bw, batch)));
     return inv_fst_split(p->t, rc, ic, grid, batch, precision, p->work.ptr, (cudaStream_t)stream);
+}
+
+int s2g_fst_refined(s2g_plan p, const double* grid, double* rc, double* ic, int batch, int precision,
+                    void* stream) {
+    S2G_TRY(plan_check(p, batch));
+    if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(p->work.ensure(refine_work_bytes(p->bw, batch)));
+    S2G_TRY(p->io.ensure(refine_io_bytes(p->bw, batch)));
+    return fst_refined(p->t, grid, rc, ic, batch, precision, p->io.ptr, p->work.ptr, (cudaStream_t)stream);
+}
+
+int s2g_inv_fst_refined(s2g_plan p, const double* rc, const double* ic, double* grid, int batch, int precision,
+                        void* stream) {
+    S2G_TRY(plan_check(p, batch));
+    if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(p->work.ensure(refine_work_bytes(p->bw, batch)));
+    S2G_TRY(p->io.ensure(refine_io_bytes(p->bw, batch)));
+    return inv_fst_refined(p->t, rc, ic, grid, batch, precision, p->io.ptr, p->work.ptr, (cudaStream_t)stream);
 }
 
 int s2g_plan_sync_status(s2g_plan p) {

@@ -1,0 +1,566 @@
+// group.cu -- grouped real-field transforms of many functions of uneven bandwidth.
+//
+// A group fixes a list of functions (function f has bandwidth bw[f], a power of two in
+// [16, 512]) and a split precision.  Functions are binned by bandwidth into classes; each
+// class owns class-contiguous intermediate arrays.  One transform runs as
+//   forward : per class (on its own forked stream) the phi-DFT and the weighted DCT-II
+//             (FST_semi_memo.c:81-90, seminaive.c:161-176), then ONE persistent tcgen05
+//             contraction launch over the work items of every class (seminaive.c:183-197);
+//   inverse : ONE persistent contraction launch (seminaive.c:74-98), then per class the
+//             DCT-III, naive-order recombination and DFT over the orders (FST_semi_memo.c:334-350).
+// The sequence is captured once as a CUDA graph (on an internal stream, with the class
+// stages as parallel branches) and replayed on the caller's stream; the first call with a
+// given set of pointers runs eagerly and captures, later calls replay.
+//
+// Tile shapes (the N extent of each class's contraction tile, CTAs per SM of the persistent
+// kernel) come from an autotuner that times candidate shapes on the group's own sizes and
+// keeps the fastest; results are cached per (device, precision, class sizes) in memory and,
+// when $S2G_TUNE_CACHE names a file, on disk.
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "s2g_internal.h"
+
+namespace s2g {
+
+static constexpr int kGroupMaxClasses = 6;
+
+struct GroupClass {
+    int B = 0, N = 0, NB = 0;
+    Tables* t = nullptr;
+    std::vector<int> funcs;     // member functions, in the caller's order
+    int64_t* gmap = nullptr;    // device: member i -> grid offset (elements)
+    int64_t* cmap = nullptr;    // device: member i -> coefficient offset
+    float* buf0 = nullptr;      // X (forward) / F (inverse): [2][N][B][2B]
+    float* buf1 = nullptr;      // C (forward) / Fc (inverse): [2][N][B][B]
+};
+
+struct GroupGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void* ptr[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    unsigned long long kernels = 0;
+};
+
+}  // namespace s2g
+
+struct s2g_group_s {
+    int device = -1, precision = 0, nfunc = 0;
+    std::vector<int> bw;
+    std::vector<int64_t> goff, coff;
+    int64_t grid_total = 0, coef_total = 0;
+    std::vector<s2g::GroupClass> cls;
+    void* mem = nullptr;        // one device allocation: maps, intermediates, counters
+    int* counters = nullptr;    // [0] forward, [1] inverse contraction work counters
+    int ctas_per_sm = 0;        // 0: as many as fit
+    cudaStream_t cap = nullptr;
+    cudaStream_t side[s2g::kGroupMaxClasses] = {};
+    cudaEvent_t fork = nullptr, mid = nullptr, join[s2g::kGroupMaxClasses] = {};
+    s2g::GroupGraph graphs[3];  // forward, inverse, forward+inverse
+    std::string tuning;         // description of the chosen tile shapes
+};
+
+namespace s2g {
+
+// ---- launch sequences (eager or under capture) ----
+
+static int group_fwd_seq(s2g_group g, const float* grid, float* rc, float* ic, cudaStream_t st) {
+    S2G_CUDA(cudaEventRecord(g->fork, st));
+    const int nc = (int)g->cls.size();
+    for (int c = 0; c < nc; ++c) {
+        GroupClass& k = g->cls[c];
+        cudaStream_t s = g->side[c];
+        S2G_CUDA(cudaStreamWaitEvent(s, g->fork, 0));
+        S2G_TRY(split_fwd_head(k.t, grid, k.buf0, k.buf1, k.N, k.gmap, s));
+        S2G_CUDA(cudaEventRecord(g->join[c], s));
+        S2G_CUDA(cudaStreamWaitEvent(st, g->join[c], 0));
+    }
+    LegSpec spec[kGroupMaxClasses] = {};
+    for (int c = 0; c < nc; ++c) {
+        GroupClass& k = g->cls[c];
+        LegSpec& q = spec[c];
+        q.t = k.t;
+        q.N = k.N;
+        q.NB = k.NB;
+        q.C = k.buf1;
+        q.X = k.buf0;
+        q.rc = rc;
+        q.ic = ic;
+        q.cmap = k.cmap;
+    }
+    return split_leg(true, g->precision, spec, nc, g->counters, g->ctas_per_sm, st);
+}
+
+static int group_inv_seq(s2g_group g, const float* rc, const float* ic, float* grid, cudaStream_t st) {
+    const int nc = (int)g->cls.size();
+    LegSpec spec[kGroupMaxClasses] = {};
+    for (int c = 0; c < nc; ++c) {
+        GroupClass& k = g->cls[c];
+        LegSpec& q = spec[c];
+        q.t = k.t;
+        q.N = k.N;
+        q.NB = k.NB;
+        q.rc_in = rc;
+        q.ic_in = ic;
+        q.Fc = k.buf1;
+        q.F = k.buf0;
+        q.cmap = k.cmap;
+    }
+    S2G_TRY(split_leg(false, g->precision, spec, nc, g->counters + 1, g->ctas_per_sm, st));
+    S2G_CUDA(cudaEventRecord(g->mid, st));
+    for (int c = 0; c < nc; ++c) {
+        GroupClass& k = g->cls[c];
+        cudaStream_t s = g->side[c];
+        S2G_CUDA(cudaStreamWaitEvent(s, g->mid, 0));
+        S2G_TRY(split_inv_tail(k.t, k.buf0, k.buf1, grid, k.N, k.gmap, s));
+        S2G_CUDA(cudaEventRecord(g->join[c], s));
+        S2G_CUDA(cudaStreamWaitEvent(st, g->join[c], 0));
+    }
+    return S2G_OK;
+}
+
+static int group_seq(s2g_group g, int kind, const void* const* ptr, cudaStream_t st) {
+    if (kind == 0) return group_fwd_seq(g, (const float*)ptr[0], (float*)ptr[1], (float*)ptr[2], st);
+    if (kind == 1) return group_inv_seq(g, (const float*)ptr[0], (const float*)ptr[1], (float*)ptr[2], st);
+    S2G_TRY(group_fwd_seq(g, (const float*)ptr[0], (float*)ptr[1], (float*)ptr[2], st));
+    return group_inv_seq(g, (const float*)ptr[1], (const float*)ptr[2], (float*)ptr[3], st);
+}
+
+static void drop_graph(GroupGraph& gr) {
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    gr = GroupGraph{};
+}
+
+// Runs sequence `kind` on `st`: replays its graph when the pointers match the captured ones;
+// otherwise runs eagerly on `st` and captures a new graph (on the internal stream) for later calls.
+static int group_run(s2g_group g, int kind, const void* const* ptr, int nptr, cudaStream_t st) {
+    GroupGraph& gr = g->graphs[kind];
+    bool same = gr.exec != nullptr;
+    for (int i = 0; i < nptr && same; ++i) same = gr.ptr[i] == ptr[i];
+    if (same) {
+        S2G_CUDA(cudaGraphLaunch(gr.exec, st));
+        launches_add(gr.kernels);
+        return S2G_OK;
+    }
+    drop_graph(gr);
+    S2G_TRY(group_seq(g, kind, ptr, st));
+    // capture for the next call with these pointers (the capture runs nothing)
+    cudaGraph_t graph = nullptr;
+    S2G_CUDA(cudaStreamBeginCapture(g->cap, cudaStreamCaptureModeThreadLocal));
+    capture_count_begin();
+    const int r = group_seq(g, kind, ptr, g->cap);
+    const unsigned long long nk = capture_count_end();
+    const cudaError_t e = cudaStreamEndCapture(g->cap, &graph);
+    if (r != S2G_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return r;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    const cudaError_t ei = cudaGraphInstantiate(&gr.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        gr.exec = nullptr;
+        return cuda_fail(ei, "cudaGraphInstantiate");
+    }
+    for (int i = 0; i < nptr; ++i) gr.ptr[i] = ptr[i];
+    gr.kernels = nk;
+    return S2G_OK;
+}
+
+// ---- autotuner ----
+
+static std::mutex g_tune_mu;
+static std::map<std::string, std::string> g_tune;  // key -> "cps NB0 NB1 ..."
+static bool g_tune_loaded = false;
+
+static std::string tune_key(s2g_group g) {
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, g->device);
+    std::string k = std::string(prop.name) + "|p" + std::to_string(g->precision);
+    for (auto& c : g->cls) k += "|" + std::to_string(c.B) + "x" + std::to_string(c.N);
+    for (auto& ch : k)
+        if (ch == ' ') ch = '_';
+    return k;
+}
+
+static void tune_load() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = getenv("S2G_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE* f = fopen(path, "r");
+    if (!f) return;
+    char line[1024];
+    while (fgets(line, sizeof line, f)) {
+        char* sp = strchr(line, ' ');
+        if (!sp) continue;
+        *sp = 0;
+        std::string v(sp + 1);
+        while (!v.empty() && (v.back() == '\n' || v.back() == '\r')) v.pop_back();
+        g_tune[line] = v;
+    }
+    fclose(f);
+}
+
+static void tune_store(const std::string& key, const std::string& val) {
+    g_tune[key] = val;
+    const char* path = getenv("S2G_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE* f = fopen(path, "a");
+    if (!f) return;
+    fprintf(f, "%s %s\n", key.c_str(), val.c_str());
+    fclose(f);
+}
+
+static std::string tune_value(s2g_group g) {
+    std::string v = std::to_string(g->ctas_per_sm);
+    for (auto& c : g->cls) v += " " + std::to_string(c.NB);
+    return v;
+}
+
+static bool tune_apply(s2g_group g, const std::string& v) {
+    std::vector<int> x;
+    const char* p = v.c_str();
+    char* end = nullptr;
+    for (;;) {
+        const long a = strtol(p, &end, 10);
+        if (end == p) break;
+        x.push_back((int)a);
+        p = end;
+    }
+    if (x.size() != g->cls.size() + 1) return false;
+    g->ctas_per_sm = x[0];
+    for (size_t c = 0; c < g->cls.size(); ++c) g->cls[c].NB = x[c + 1];
+    return true;
+}
+
+static void tune_describe(s2g_group g) {
+    std::string d = "{\"ctas_per_sm\": " + std::to_string(g->ctas_per_sm) + ", \"tile_n\": {";
+    for (size_t c = 0; c < g->cls.size(); ++c) {
+        if (c) d += ", ";
+        d += "\"" + std::to_string(g->cls[c].B) + "\": " + std::to_string(g->cls[c].NB);
+    }
+    g->tuning = d + "}}";
+}
+
+// Candidate N extents of a class's contraction tile: the whole table-row extent and its
+// halvings down to 32 (multiples of 16).
+static std::vector<int> nb_candidates(int B) {
+    const int full = std::max(16, ((B / 2) + 15) & ~15);
+    std::vector<int> v{0};
+    for (int n = full / 2; n >= 32; n /= 2) v.push_back(n);
+    return v;
+}
+
+// Times forward + inverse contraction launches with the current shapes (ms, best of reps).
+static int time_contractions(s2g_group g, const float* grid, float* rc, float* ic, int reps, float* ms) {
+    cudaEvent_t a, b;
+    S2G_CUDA(cudaEventCreate(&a));
+    S2G_CUDA(cudaEventCreate(&b));
+    float best = 1e30f;
+    int r = S2G_OK;
+    const int nc = (int)g->cls.size();
+    for (int it = 0; it < reps + 1 && r == S2G_OK; ++it) {
+        LegSpec f[kGroupMaxClasses] = {}, iv[kGroupMaxClasses] = {};
+        for (int c = 0; c < nc; ++c) {
+            GroupClass& k = g->cls[c];
+            f[c] = LegSpec{k.t, k.N, k.NB, k.buf1, k.buf0, nullptr, nullptr, rc, ic, nullptr, nullptr, k.cmap};
+            iv[c] = LegSpec{k.t, k.N, k.NB, nullptr, nullptr, rc, ic, nullptr, nullptr, k.buf1, k.buf0, k.cmap};
+        }
+        cudaEventRecord(a, g->cap);
+        r = split_leg(true, g->precision, f, nc, g->counters, g->ctas_per_sm, g->cap);
+        if (r == S2G_OK) r = split_leg(false, g->precision, iv, nc, g->counters + 1, g->ctas_per_sm, g->cap);
+        cudaEventRecord(b, g->cap);
+        if (cudaEventSynchronize(b) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "autotune");
+        float t = 0;
+        cudaEventElapsedTime(&t, a, b);
+        if (it > 0) best = std::min(best, t);  // first run warms caches
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    (void)grid;
+    *ms = best;
+    return r;
+}
+
+static int group_autotune(s2g_group g, int force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load();
+    const std::string key = tune_key(g);
+    if (!force) {
+        auto it = g_tune.find(key);
+        if (it != g_tune.end() && tune_apply(g, it->second)) {
+            tune_describe(g);
+            return S2G_OK;
+        }
+    }
+    // synthetic coefficients and intermediates: the contraction's cost does not depend on values
+    float* rc = nullptr;
+    S2G_CUDA(cudaMalloc(&rc, 2 * sizeof(float) * (size_t)g->coef_total));
+    float* ic = rc + g->coef_total;
+    S2G_CUDA(cudaMemsetAsync(rc, 0, 2 * sizeof(float) * (size_t)g->coef_total, g->cap));
+    for (auto& c : g->cls) {
+        S2G_CUDA(cudaMemsetAsync(c.buf0, 0, sizeof(float) * 2 * (size_t)c.N * c.B * 2 * c.B, g->cap));
+        S2G_CUDA(cudaMemsetAsync(c.buf1, 0, sizeof(float) * 2 * (size_t)c.N * c.B * c.B, g->cap));
+    }
+    int r = S2G_OK;
+    float best = 0;
+    g->ctas_per_sm = 0;
+    for (auto& c : g->cls) c.NB = 0;
+    r = time_contractions(g, nullptr, rc, ic, 3, &best);
+    // coordinate descent: classes with the most work first, then the persistent grid size
+    std::vector<int> order(g->cls.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+        const double wx = (double)g->cls[x].N * g->cls[x].B * g->cls[x].B * g->cls[x].B;
+        const double wy = (double)g->cls[y].N * g->cls[y].B * g->cls[y].B * g->cls[y].B;
+        return wx > wy;
+    });
+    for (int ci : order) {
+        if (r != S2G_OK) break;
+        GroupClass& c = g->cls[ci];
+        int keep = c.NB;
+        for (int nb : nb_candidates(c.B)) {
+            if (nb == keep) continue;
+            c.NB = nb;
+            float ms = 0;
+            r = time_contractions(g, nullptr, rc, ic, 3, &ms);
+            if (r != S2G_OK) break;
+            if (ms < best * 0.98f) best = ms, keep = nb;
+        }
+        c.NB = keep;
+    }
+    for (int cps : {1, 2, 3}) {
+        if (r != S2G_OK) break;
+        const int keep = g->ctas_per_sm;
+        g->ctas_per_sm = cps;
+        float ms = 0;
+        r = time_contractions(g, nullptr, rc, ic, 3, &ms);
+        if (r == S2G_OK && ms < best * 0.98f) best = ms;
+        else g->ctas_per_sm = keep;
+    }
+    cudaStreamSynchronize(g->cap);
+    cudaFree(rc);
+    if (r != S2G_OK) return r;
+    tune_store(key, tune_value(g));
+    tune_describe(g);
+    for (auto& gr : g->graphs) drop_graph(gr);
+    return S2G_OK;
+}
+
+static void group_free(s2g_group g) {
+    if (!g) return;
+    if (g->device >= 0) cudaSetDevice(g->device);
+    if (g->cap) cudaStreamSynchronize(g->cap);
+    for (auto& gr : g->graphs) drop_graph(gr);
+    for (auto s : g->side)
+        if (s) cudaStreamDestroy(s);
+    if (g->cap) cudaStreamDestroy(g->cap);
+    for (auto e : g->join)
+        if (e) cudaEventDestroy(e);
+    if (g->fork) cudaEventDestroy(g->fork);
+    if (g->mid) cudaEventDestroy(g->mid);
+    cudaFree(g->mem);
+    for (auto& c : g->cls) put_tables(c.t);
+    delete g;
+}
+
+}  // namespace s2g
+
+using namespace s2g;
+
+extern "C" {
+
+int s2g_group_create(s2g_group* out, int nfunc, const int* bw, int precision) {
+    if (!out) return fail(S2G_ERR_ARG, "NULL group pointer");
+    *out = nullptr;
+    if (nfunc < 1 || !bw) return fail(S2G_ERR_ARG, "a group needs nfunc >= 1 bandwidths (got %d)", nfunc);
+    if (precision != S2G_PREC_BF16X3 && precision != S2G_PREC_BF16X2 && precision != S2G_PREC_FP16X2)
+        return fail(S2G_ERR_ARG, "precision %d is not a split (tensor-core) mode", precision);
+    for (int f = 0; f < nfunc; ++f)
+        if (bw[f] < 16 || bw[f] > 512 || (bw[f] & (bw[f] - 1)))
+            return fail(S2G_ERR_UNSUPPORTED, "function %d: bandwidth %d is not a power of two in [16, 512]", f,
+                        bw[f]);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(S2G_ERR_NOGPU, "no CUDA device");
+    s2g_group g = new s2g_group_s();
+    g->device = dev;
+    g->precision = precision;
+    g->nfunc = nfunc;
+    g->bw.assign(bw, bw + nfunc);
+    g->goff.resize(nfunc);
+    g->coff.resize(nfunc);
+    for (int f = 0; f < nfunc; ++f) {
+        g->goff[f] = g->grid_total;
+        g->coff[f] = g->coef_total;
+        g->grid_total += 4 * (int64_t)bw[f] * bw[f];
+        g->coef_total += (int64_t)bw[f] * bw[f];
+    }
+    // classes in increasing bandwidth
+    for (int B = 16; B <= 512; B *= 2) {
+        GroupClass c;
+        c.B = B;
+        for (int f = 0; f < nfunc; ++f)
+            if (bw[f] == B) c.funcs.push_back(f);
+        if (c.funcs.empty()) continue;
+        c.N = (int)c.funcs.size();
+        g->cls.push_back(c);
+    }
+    int r = S2G_OK;
+    for (auto& c : g->cls) {
+        if (r == S2G_OK) r = get_tables(c.B, c.B, &c.t);
+        else c.t = nullptr;
+    }
+    // device memory: maps, intermediates (256-byte aligned pieces), two counters
+    auto rnd = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t total = 256;
+    for (auto& c : g->cls) {
+        total += 2 * rnd(sizeof(int64_t) * c.N);
+        total += rnd(sizeof(float) * 2 * (size_t)c.N * c.B * 2 * c.B) + rnd(sizeof(float) * 2 * (size_t)c.N * c.B * c.B);
+    }
+    if (r == S2G_OK && cudaMalloc(&g->mem, total) != cudaSuccess)
+        r = fail(S2G_ERR_NOMEM, "group: cudaMalloc of %zu bytes failed", total);
+    if (r == S2G_OK) {
+        char* p = (char*)g->mem;
+        g->counters = (int*)p;
+        p += 256;
+        std::vector<int64_t> gm, cm;
+        for (auto& c : g->cls) {
+            c.gmap = (int64_t*)p;
+            p += rnd(sizeof(int64_t) * c.N);
+            c.cmap = (int64_t*)p;
+            p += rnd(sizeof(int64_t) * c.N);
+            c.buf0 = (float*)p;
+            p += rnd(sizeof(float) * 2 * (size_t)c.N * c.B * 2 * c.B);
+            c.buf1 = (float*)p;
+            p += rnd(sizeof(float) * 2 * (size_t)c.N * c.B * c.B);
+            gm.clear();
+            cm.clear();
+            for (int f : c.funcs) gm.push_back(g->goff[f]), cm.push_back(g->coff[f]);
+            if (cudaMemcpy(c.gmap, gm.data(), sizeof(int64_t) * c.N, cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(c.cmap, cm.data(), sizeof(int64_t) * c.N, cudaMemcpyHostToDevice) != cudaSuccess) {
+                r = cuda_fail(cudaGetLastError(), "group maps");
+                break;
+            }
+        }
+    }
+    auto ck = [&](cudaError_t e, const char* w) {
+        if (e != cudaSuccess && r == S2G_OK) r = cuda_fail(e, w);
+    };
+    if (r == S2G_OK) {
+        ck(cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (size_t c = 0; c < g->cls.size(); ++c)
+            ck(cudaStreamCreateWithFlags(&g->side[c], cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&g->mid, cudaEventDisableTiming), "cudaEventCreate");
+        for (size_t c = 0; c < g->cls.size(); ++c)
+            ck(cudaEventCreateWithFlags(&g->join[c], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    // operands packed now, so that no later call allocates (a graph capture cannot)
+    for (auto& c : g->cls)
+        if (r == S2G_OK) r = split_prepare(c.t, precision);
+    if (r != S2G_OK) {
+        group_free(g);
+        return r;
+    }
+    tune_describe(g);
+    *out = g;
+    return S2G_OK;
+}
+
+int s2g_group_destroy(s2g_group g) {
+    group_free(g);
+    return S2G_OK;
+}
+
+int s2g_group_layout(s2g_group g, int64_t* grid_offsets, int64_t* coeff_offsets, int64_t* grid_total,
+                     int64_t* coeff_total) {
+    if (!g) return fail(S2G_ERR_ARG, "NULL group");
+    if (grid_offsets) memcpy(grid_offsets, g->goff.data(), sizeof(int64_t) * g->nfunc);
+    if (coeff_offsets) memcpy(coeff_offsets, g->coff.data(), sizeof(int64_t) * g->nfunc);
+    if (grid_total) *grid_total = g->grid_total;
+    if (coeff_total) *coeff_total = g->coef_total;
+    return S2G_OK;
+}
+
+static int group_check(s2g_group g) {
+    if (!g) return fail(S2G_ERR_ARG, "NULL group");
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(S2G_ERR_NOGPU, "no CUDA device");
+    if (dev != g->device) return fail(S2G_ERR_ARG, "group made on device %d used on device %d", g->device, dev);
+    return S2G_OK;
+}
+
+int s2g_group_fst(s2g_group g, const float* grid, float* rcoeffs, float* icoeffs, void* stream) {
+    S2G_TRY(group_check(g));
+    if (!grid || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
+    const void* p[3] = {grid, rcoeffs, icoeffs};
+    return group_run(g, 0, p, 3, (cudaStream_t)stream);
+}
+
+int s2g_group_inv_fst(s2g_group g, const float* rcoeffs, const float* icoeffs, float* grid, void* stream) {
+    S2G_TRY(group_check(g));
+    if (!grid || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
+    const void* p[3] = {rcoeffs, icoeffs, grid};
+    return group_run(g, 1, p, 3, (cudaStream_t)stream);
+}
+
+int s2g_group_fst_inv(s2g_group g, const float* grid, float* rcoeffs, float* icoeffs, float* grid_out,
+                      void* stream) {
+    S2G_TRY(group_check(g));
+    if (!grid || !rcoeffs || !icoeffs || !grid_out) return fail(S2G_ERR_ARG, "NULL argument");
+    const void* p[4] = {grid, rcoeffs, icoeffs, grid_out};
+    return group_run(g, 2, p, 4, (cudaStream_t)stream);
+}
+
+int s2g_group_autotune(s2g_group g, int force) {
+    S2G_TRY(group_check(g));
+    return group_autotune(g, force);
+}
+
+int s2g_group_set_tiles(s2g_group g, int ctas_per_sm, const int* tile_n) {
+    S2G_TRY(group_check(g));
+    if (ctas_per_sm < 0 || ctas_per_sm > 8) return fail(S2G_ERR_ARG, "ctas_per_sm %d outside [0, 8]", ctas_per_sm);
+    for (size_t c = 0; tile_n && c < g->cls.size(); ++c)
+        if (tile_n[c] < 0 || tile_n[c] > 256 || tile_n[c] % 16)
+            return fail(S2G_ERR_ARG, "tile_n[%zu] = %d: a multiple of 16 in [0, 256]", c, tile_n[c]);
+    g->ctas_per_sm = ctas_per_sm;
+    for (size_t c = 0; c < g->cls.size(); ++c) g->cls[c].NB = tile_n ? tile_n[c] : 0;
+    for (auto& gr : g->graphs) drop_graph(gr);
+    tune_describe(g);
+    return S2G_OK;
+}
+
+int s2g_group_describe(s2g_group g, char* buf, size_t len) {
+    if (!g || !buf || len == 0) return fail(S2G_ERR_ARG, "NULL argument");
+    std::string d = "{\"classes\": [";
+    for (size_t c = 0; c < g->cls.size(); ++c) {
+        if (c) d += ", ";
+        d += "[" + std::to_string(g->cls[c].B) + ", " + std::to_string(g->cls[c].N) + "]";
+    }
+    d += "], \"tiles\": " + g->tuning + ", \"graph_kernels\": [" + std::to_string(g->graphs[0].kernels) + ", " +
+         std::to_string(g->graphs[1].kernels) + ", " + std::to_string(g->graphs[2].kernels) + "]}";
+    if (d.size() + 1 > len) return fail(S2G_ERR_ARG, "buffer of %zu bytes too small (%zu needed)", len, d.size() + 1);
+    memcpy(buf, d.c_str(), d.size() + 1);
+    return S2G_OK;
+}
+
+int s2g_group_sync_status(s2g_group g) {
+    S2G_TRY(group_check(g));
+    S2G_CUDA(cudaStreamSynchronize(g->cap));
+    S2G_CUDA(cudaDeviceSynchronize());
+    int r = S2G_OK;
+    for (auto& c : g->cls) {
+        const int v = split_device_status(c.t, 1);
+        if (v != S2G_OK && r == S2G_OK) r = v;
+    }
+    return r;
+}
+
+}  // extern "C"

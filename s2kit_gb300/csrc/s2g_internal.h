@@ -33,6 +33,11 @@ int cuda_fail(cudaError_t e, const char* what);
 void prof_begin(const char* name, cudaStream_t st);
 void prof_end(cudaStream_t st);
 
+// Graph capture on this thread: launches counted into the graph (see launches_add for replays).
+void capture_count_begin();
+unsigned long long capture_count_end();
+void launches_add(unsigned long long n);
+
 struct ProfScope {
     cudaStream_t st;
     ProfScope(const char* name, cudaStream_t s) : st(s) { prof_begin(name, s); }
@@ -53,6 +58,7 @@ struct Tables {
     double2* tw_D = nullptr;    // exp(i pi k / (2 * 2bw)), k < 2bw (DCT pre/post twiddle)
     // split-precision (tensor core) operands, built on first use
     void* split = nullptr;
+    int refs = 0;               // references (cache, plans, groups, calls in flight); under the cache lock
 };
 
 // Device scratch owned by a plan; grown on demand.
@@ -63,8 +69,14 @@ struct Scratch {
     void release();
 };
 
-// Build / fetch device tables (cached per device, bw, cutoff).
+// Build / fetch device tables (cached per device, bw, cutoff); the caller gets a reference and
+// returns it with put_tables.
 int get_tables(int bw, int cutoff, Tables** out);
+void put_tables(Tables* t);
+struct TabRef {
+    Tables* t;
+    ~TabRef() { put_tables(t); }
+};
 // Build tables into caller-visible device buffers (used by the host table builders).
 int build_tables(Tables* t, cudaStream_t st);
 int generate_weights_device(int bw, double* d_weights, cudaStream_t st);
@@ -110,5 +122,39 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
                   cudaStream_t st);
 // Reads (and optionally clears) the device error word of the tensor-core kernels.
 int split_device_status(Tables* t, int clear);
+
+// One bandwidth class of a (grouped) tensor-core contraction launch.  Intermediate arrays are
+// class-contiguous: X/F [2][N][B][2B], C/Fc [2][N][B][B] floats.
+struct LegSpec {
+    Tables* t;
+    int N;                    // functions of this class
+    int NB;                   // table rows per work item (0: the largest the class needs)
+    const float* C;           // forward: DCT output
+    const float* X;           // forward: phi-DFT output (naive orders)
+    const float* rc_in;       // inverse: input coefficients
+    const float* ic_in;
+    float* rc;                // forward: output coefficients
+    float* ic;
+    float* Fc;                // inverse: cosine-series output
+    float* F;                 // inverse: naive-order output
+    const int64_t* cmap;      // function -> coefficient offset (null: f * B * B)
+};
+// One persistent launch over every class; counter: one device int (zeroed on `st` here);
+// ctas_per_sm 0 = as many as fit.
+int split_leg(bool fwd, int precision, const LegSpec* cls, int ncls, int* counter, int ctas_per_sm,
+              cudaStream_t st);
+// Packs the tensor-core operands of `t` for `precision` now (they are otherwise packed on first use).
+int split_prepare(Tables* t, int precision);
+int split_fwd_head(Tables* t, const float* grid, float* X, float* C, int batch, const int64_t* gmap,
+                   cudaStream_t st);
+int split_inv_tail(Tables* t, float* F, float* Fc, float* grid, int batch, const int64_t* gmap, cudaStream_t st);
+
+// ---- split transforms with one FP64-residual refinement step (refine.cu) ----
+size_t refine_io_bytes(int bw, int batch);
+size_t refine_work_bytes(int bw, int batch);
+int fst_refined(Tables* t, const double* grid, double* rc, double* ic, int batch, int precision, void* io,
+                void* work, cudaStream_t st);
+int inv_fst_refined(Tables* t, const double* rc, const double* ic, double* grid, int batch, int precision, void* io,
+                    void* work, cudaStream_t st);
 
 }  // namespace s2g

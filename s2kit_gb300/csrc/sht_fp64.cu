@@ -51,7 +51,8 @@ int twiddles_device(int n, double2* d_full, double2* d_quarter, cudaStream_t st)
 }
 
 static int set_smem(const void* fn, size_t bytes) {
-    if (bytes > 48 * 1024) S2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    // always set: the 48 KiB default covers static plus dynamic shared memory
+    S2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return S2G_OK;
 }
 

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -45,6 +46,14 @@ struct Split {
     uint8_t* inv_blob = nullptr;
     int64_t* fwd_off = nullptr;  // device, bytes, per order
     int64_t* inv_off = nullptr;
+    // FP16 two-term blobs (built on first use), table scaled by tab16 = 2^k
+    uint8_t* fwd16 = nullptr;
+    uint8_t* inv16 = nullptr;
+    int64_t* fwd16_off = nullptr;
+    int64_t* inv16_off = nullptr;
+    double tab16 = 0.0;
+    // per (direction, tile N): prefix sums over m of the contraction's work items per order
+    std::vector<std::pair<int, int*>> mstart[2];
     int* err = nullptr;          // device error word (S2G_ERR_TIMEOUT on an expired wait)
     size_t fwd_bytes = 0, inv_bytes = 0;
 };
@@ -62,6 +71,12 @@ void free_split(Tables* t) {
     cudaFree(s->inv_blob);
     cudaFree(s->fwd_off);
     cudaFree(s->inv_off);
+    cudaFree(s->fwd16);
+    cudaFree(s->inv16);
+    cudaFree(s->fwd16_off);
+    cudaFree(s->inv16_off);
+    for (auto& v : s->mstart)
+        for (auto& e : v) cudaFree(e.second);
     cudaFree(s->err);
     delete s;
     t->split = nullptr;
@@ -104,14 +119,15 @@ __host__ __device__ __forceinline__ Geo geo(bool fwd, int B, int m) {
     return g;
 }
 
-__host__ __device__ __forceinline__ int64_t blob_bytes(bool fwd, int B, int m) {
+__host__ __device__ __forceinline__ int64_t blob_bytes(bool fwd, int B, int m, int nterms) {
     const Geo g = geo(fwd, B, m);
-    return (int64_t)2 * g.nblk * g.nch * 3 * g.NP * kKC * 2;
+    return (int64_t)2 * g.nblk * g.nch * nterms * g.NP * kKC * 2;
 }
 
 // ------------------------------------------------------------------------------------
-// Operand packing: table operands in the tcgen05 smem layout, three BF16 terms, one
-// contiguous blob per (order, parity, latitude block, K-chunk): [term][NP rows][KC].
+// Operand packing: table operands in the tcgen05 smem layout, one contiguous blob per
+// (order, parity, latitude block, K-chunk): [term][NP rows][KC], three BF16 terms or two FP16
+// terms of the table scaled by a power of two.
 //   forward seminaive : rows i (l = m+t+2i), cols j (cosine frequency k = 2j+t)
 //   forward naive     : rows i, cols j (latitude j < B): P(m,l)(x_j) w_j  (even/odd folded)
 //   inverse seminaive : rows j, cols i
@@ -139,10 +155,15 @@ struct Pack {
     const double* w;        // quadrature weights
     uint8_t* blob;
     const int64_t* blob_off;
+    double scale;           // FP16 terms: table scale
+    unsigned long long* maxbits;  // kPackMax: largest |entry| as the bits of a double
 };
 
-template <bool FWD>
+enum { kPackBF16 = 0, kPackMax = 1, kPackF16 = 2 };
+
+template <bool FWD, int MODE>
 __global__ void k_pack(Pack p) {
+    constexpr int NT = MODE == kPackF16 ? 2 : 3;
     const int B = p.B, S = 2 * B;
     const int m = blockIdx.x, c = blockIdx.y;
     const int t = blockIdx.z & 1, nb = blockIdx.z >> 1;
@@ -150,9 +171,11 @@ __global__ void k_pack(Pack p) {
     if (c >= g.nch || nb >= g.nblk) return;
     const bool nv = naive_order(m);
     const size_t tile = (size_t)g.NP * kKC * 2;
-    uint8_t* out = p.blob + p.blob_off[m] + ((size_t)(t * g.nblk + nb) * g.nch + c) * 3 * tile;
+    uint8_t* out = MODE == kPackMax ? nullptr
+                                    : p.blob + p.blob_off[m] + ((size_t)(t * g.nblk + nb) * g.nch + c) * NT * tile;
     const double* tab = p.fwd + p.off[m];
     const double* pml = nv ? p.pml + p.pml_off[m] : nullptr;
+    double mx = 0.0;
     for (int e = threadIdx.x; e < g.NP * kKC; e += blockDim.x) {
         const int n = e / kKC, kk = e - n * kKC;
         const int kidx = c * kKC + kk;
@@ -169,10 +192,21 @@ __global__ void k_pack(Pack p) {
                 if (l < B && th < B) v = pml[(size_t)(l - m) * S + th];
             }
         }
-        __nv_bfloat16 h[3];
-        split3d(v, h);
-        for (int s = 0; s < 3; ++s) *(__nv_bfloat16*)(out + s * tile + tc::tile_off(n, kk, kKC)) = h[s];
+        if (MODE == kPackMax) {
+            mx = fmax(mx, fabs(v));
+        } else if (MODE == kPackF16) {
+            const double x = v * p.scale;
+            const __half h0 = __double2half(x);
+            const __half h1 = __double2half(x - (double)__half2float(h0));
+            *(__half*)(out + tc::tile_off(n, kk, kKC)) = h0;
+            *(__half*)(out + tile + tc::tile_off(n, kk, kKC)) = h1;
+        } else {
+            __nv_bfloat16 h[3];
+            split3d(v, h);
+            for (int s = 0; s < 3; ++s) *(__nv_bfloat16*)(out + s * tile + tc::tile_off(n, kk, kKC)) = h[s];
+        }
     }
+    if (MODE == kPackMax && mx > 0.0) atomicMax(p.maxbits, (unsigned long long)__double_as_longlong(mx));
 }
 
 __global__ void k_to_f32(const double* a, float* b, int n) {
@@ -185,54 +219,128 @@ __global__ void k_tw_f32(const double2* a, float2* b, int n) {
     if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
 }
 
-static int build_split(Tables* t) {
-    std::lock_guard<std::mutex> lk(g_split_mu);
-    if (t->split) return S2G_OK;
-    const int B = t->bw, S = 2 * B;
-    if ((B & (B - 1)) || B < 16 || B > 512)
-        return fail(S2G_ERR_UNSUPPORTED, "split-precision path needs a power-of-two bw in [16, 512] (got %d)", B);
-    if (t->cutoff != B) return fail(S2G_ERR_UNSUPPORTED, "split-precision path is seminaive at every order (cutoff == bw)");
-    Split* s = new Split();
-    s->B = B;
-    s->KC = kKC;
+// Packs both directions' table blobs of `t` into s (BF16: three terms; FP16: two terms of the
+// table scaled by 2^k, k chosen from the largest entry so that it stays below 2^14).
+static int pack_blobs(Tables* t, Split* s, bool f16, cudaStream_t st) {
+    const int B = t->bw, S = 2 * B, nt = f16 ? 2 : 3;
     std::vector<int64_t> fo(B), io(B), po(B, 0);
     int64_t fb = 0, ib = 0, pb = 0;
     for (int m = 0; m < B; ++m) {
         fo[m] = fb;
         io[m] = ib;
-        fb += blob_bytes(true, B, m);
-        ib += blob_bytes(false, B, m);
+        fb += blob_bytes(true, B, m, nt);
+        ib += blob_bytes(false, B, m, nt);
         if (naive_order(m)) {
             po[m] = pb;
             pb += (int64_t)(B - m) * S;
         }
     }
-    s->fwd_bytes = fb;
-    s->inv_bytes = ib;
-    cudaStream_t st;
-    S2G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    uint8_t*& fblob = f16 ? s->fwd16 : s->fwd_blob;
+    uint8_t*& iblob = f16 ? s->inv16 : s->inv_blob;
+    int64_t*& foff = f16 ? s->fwd16_off : s->fwd_off;
+    int64_t*& ioff = f16 ? s->inv16_off : s->inv_off;
     int r = S2G_OK;
     auto ck = [&](cudaError_t e, const char* w) {
         if (e != cudaSuccess && r == S2G_OK) r = cuda_fail(e, w);
     };
     double* pml = nullptr;
     int64_t* d_po = nullptr;
+    unsigned long long* d_max = nullptr;
+    ck(cudaMalloc(&fblob, fb), "cudaMalloc");
+    ck(cudaMalloc(&iblob, ib), "cudaMalloc");
+    ck(cudaMalloc(&foff, sizeof(int64_t) * B), "cudaMalloc");
+    ck(cudaMalloc(&ioff, sizeof(int64_t) * B), "cudaMalloc");
+    ck(cudaMalloc(&pml, sizeof(double) * (size_t)(pb > 0 ? pb : 1)), "cudaMalloc");
+    ck(cudaMalloc(&d_po, sizeof(int64_t) * B), "cudaMalloc");
+    ck(cudaMalloc(&d_max, sizeof(unsigned long long)), "cudaMalloc");
+    if (r == S2G_OK) {
+        ck(cudaMemcpyAsync(foff, fo.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
+        ck(cudaMemcpyAsync(ioff, io.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
+        ck(cudaMemcpyAsync(d_po, po.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
+        ck(cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), st), "memset");
+    }
+    // sampled P(m,l) of the naive orders (pml.c:41-79), one order at a time
+    for (int m = 1; r == S2G_OK && m < B && m < kNaiveOddBelow; m += 2) {
+        int rr = generate_pml_device(B, m, m + 1, pml, d_po, st);
+        if (rr != S2G_OK) r = rr;
+    }
+    int fch = 0, ich = 0, iblk = 1;
+    for (int m = 0; m < B; ++m) {
+        fch = std::max(fch, geo(true, B, m).nch);
+        ich = std::max(ich, geo(false, B, m).nch);
+        iblk = std::max(iblk, geo(false, B, m).nblk);
+    }
+    const dim3 gf(B, fch, 2), gi(B, ich, 2 * iblk);
+    Pack pk{B, t->fwd, t->off, pml, d_po, t->weights, fblob, foff, 1.0, d_max};
+    if (r == S2G_OK && f16) {
+        // inverse blobs hold the same table entries as the forward ones, plus the naive samples
+        {
+            ProfScope ps_("pack_max", st);
+            k_pack<true, kPackMax><<<gf, 256, 0, st>>>(pk);
+        }
+        {
+            ProfScope ps_("pack_max", st);
+            k_pack<false, kPackMax><<<gi, 256, 0, st>>>(pk);
+        }
+        unsigned long long bits = 0;
+        ck(cudaMemcpyAsync(&bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost, st), "copy");
+        ck(cudaStreamSynchronize(st), "pack max");
+        double mx = 0.0;
+        memcpy(&mx, &bits, sizeof(mx));
+        int e = 0;
+        frexp(mx > 0.0 ? mx : 1.0, &e);  // mx < 2^e
+        s->tab16 = ldexp(1.0, 14 - e);
+        pk.scale = s->tab16;
+    }
+    if (r == S2G_OK) {
+        {
+            ProfScope ps_("pack_fwd", st);
+            if (f16) k_pack<true, kPackF16><<<gf, 256, 0, st>>>(pk);
+            else k_pack<true, kPackBF16><<<gf, 256, 0, st>>>(pk);
+        }
+        pk.blob = iblob;
+        pk.blob_off = ioff;
+        {
+            ProfScope ps_("pack_inv", st);
+            if (f16) k_pack<false, kPackF16><<<gi, 256, 0, st>>>(pk);
+            else k_pack<false, kPackBF16><<<gi, 256, 0, st>>>(pk);
+        }
+        ck(cudaGetLastError(), "pack kernels");
+        ck(cudaStreamSynchronize(st), "pack kernels");
+    }
+    cudaFree(pml);
+    cudaFree(d_po);
+    cudaFree(d_max);
+    if (!f16) {
+        s->fwd_bytes = fb;
+        s->inv_bytes = ib;
+    }
+    return r;
+}
+
+static int build_split(Tables* t) {
+    std::lock_guard<std::mutex> lk(g_split_mu);
+    if (t->split) return S2G_OK;
+    const int B = t->bw, S = 2 * B;
+    if ((B & (B - 1)) || B < 16 || B > 1024)
+        return fail(S2G_ERR_UNSUPPORTED, "split-precision path needs a power-of-two bw in [16, 1024] (got %d)", B);
+    if (t->cutoff != B) return fail(S2G_ERR_UNSUPPORTED, "split-precision path is seminaive at every order (cutoff == bw)");
+    Split* s = new Split();
+    s->B = B;
+    s->KC = kKC;
+    cudaStream_t st;
+    S2G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int r = S2G_OK;
+    auto ck = [&](cudaError_t e, const char* w) {
+        if (e != cudaSuccess && r == S2G_OK) r = cuda_fail(e, w);
+    };
     ck(cudaMalloc(&s->w32, sizeof(float) * 4 * B), "cudaMalloc");
     ck(cudaMalloc(&s->sin32, sizeof(float) * S), "cudaMalloc");
     ck(cudaMalloc(&s->twS, sizeof(float2) * S), "cudaMalloc");
     ck(cudaMalloc(&s->twD, sizeof(float2) * S), "cudaMalloc");
-    ck(cudaMalloc(&s->fwd_blob, fb), "cudaMalloc");
-    ck(cudaMalloc(&s->inv_blob, ib), "cudaMalloc");
-    ck(cudaMalloc(&s->fwd_off, sizeof(int64_t) * B), "cudaMalloc");
-    ck(cudaMalloc(&s->inv_off, sizeof(int64_t) * B), "cudaMalloc");
     ck(cudaMalloc(&s->err, sizeof(int)), "cudaMalloc");
-    ck(cudaMalloc(&pml, sizeof(double) * (size_t)(pb > 0 ? pb : 1)), "cudaMalloc");
-    ck(cudaMalloc(&d_po, sizeof(int64_t) * B), "cudaMalloc");
     if (r == S2G_OK) {
         ck(cudaMemsetAsync(s->err, 0, sizeof(int), st), "memset");
-        ck(cudaMemcpyAsync(s->fwd_off, fo.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
-        ck(cudaMemcpyAsync(s->inv_off, io.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
-        ck(cudaMemcpyAsync(d_po, po.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st), "copy");
         {
             ProfScope ps_("to_f32", st);
             k_to_f32<<<(4 * B + 255) / 256, 256, 0, st>>>(t->weights, s->w32, 4 * B);
@@ -251,39 +359,31 @@ static int build_split(Tables* t) {
         }
         ck(cudaGetLastError(), "conversion kernels");
     }
-    // sampled P(m,l) of the naive orders (pml.c:41-79), one order at a time
-    for (int m = 1; r == S2G_OK && m < B && m < kNaiveOddBelow; m += 2) {
-        int rr = generate_pml_device(B, m, m + 1, pml, d_po, st);
-        if (rr != S2G_OK) r = rr;
-    }
-    if (r == S2G_OK) {
-        Pack pk{B, t->fwd, t->off, pml, d_po, t->weights, s->fwd_blob, s->fwd_off};
-        int maxch = 0;
-        for (int m = 0; m < B; ++m) maxch = std::max(maxch, geo(true, B, m).nch);
-        {
-            ProfScope ps_("pack_fwd", st);
-            k_pack<true><<<dim3(B, maxch, 2), 256, 0, st>>>(pk);
-        }
-        pk.blob = s->inv_blob;
-        pk.blob_off = s->inv_off;
-        maxch = 0;
-        int maxblk = 1;
-        for (int m = 0; m < B; ++m) {
-            maxch = std::max(maxch, geo(false, B, m).nch);
-            maxblk = std::max(maxblk, geo(false, B, m).nblk);
-        }
-        {
-            ProfScope ps_("pack_inv", st);
-            k_pack<false><<<dim3(B, maxch, 2 * maxblk), 256, 0, st>>>(pk);
-        }
-        ck(cudaGetLastError(), "pack kernels");
-        ck(cudaStreamSynchronize(st), "pack kernels");
-    }
-    cudaFree(pml);
-    cudaFree(d_po);
+    if (r == S2G_OK) r = pack_blobs(t, s, false, st);
     cudaStreamDestroy(st);
     t->split = s;
     if (r != S2G_OK) free_split(t);
+    return r;
+}
+
+// FP16 blobs, packed on first use of S2G_PREC_FP16X2 for this table set.
+static int build_split16(Tables* t) {
+    S2G_TRY(build_split(t));
+    std::lock_guard<std::mutex> lk(g_split_mu);
+    Split* s = (Split*)t->split;
+    if (s->fwd16) return S2G_OK;
+    cudaStream_t st;
+    S2G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const int r = pack_blobs(t, s, true, st);
+    cudaStreamDestroy(st);
+    if (r != S2G_OK) {
+        cudaFree(s->fwd16);
+        cudaFree(s->inv16);
+        cudaFree(s->fwd16_off);
+        cudaFree(s->inv16_off);
+        s->fwd16 = s->inv16 = nullptr;
+        s->fwd16_off = s->inv16_off = nullptr;
+    }
     return r;
 }
 
@@ -300,13 +400,20 @@ __device__ __forceinline__ void load_tw(float2* tw, float2* twD, const float2* g
     }
 }
 
-static constexpr int kWarps = 8;       // warps per CTA in the FFT kernels
-static constexpr int kLatPerCta = 16;  // latitudes per CTA in the row kernels (2 per warp)
+// CTA shape of the FFT kernels: W warps (one sequence each), LAT = 2W latitudes per CTA in the
+// row kernels.  S = 2048 (R = 64) halves the warps so that the staging fits in shared memory.
+template <int R>
+struct FftShape {
+    static constexpr int W = R >= 64 ? 4 : 8;
+    static constexpr int LAT = 2 * W;
+    static constexpr int T = 32 * W;
+};
 
 // DFT along phi of 16 latitudes (two real rows per warp), transposed to X[p][f][m][theta], m < B.
 template <int R>
-__global__ void __launch_bounds__(256) k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N,
-                                                    float scale, const float2* __restrict__ gtw) {
+__global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N,
+                                                    float scale, const float2* __restrict__ gtw,
+                                                    const int64_t* __restrict__ gmap) {
     constexpr int S = 32 * R, B = S / 2;
     constexpr int PS = S + S / 32;        // padded spectrum length
     constexpr int RS = B + B / 32 + 1;    // padded stage row (odd)
@@ -314,16 +421,16 @@ __global__ void __launch_bounds__(256) k_rows_fwd_w(const float* __restrict__ gr
     extern __shared__ __align__(16) float fsm[];
     float2* tw = reinterpret_cast<float2*>(fsm);
     float* spr = fsm + 2 * TWL;                    // [warps][PS] re
-    float* spi = spr + kWarps * PS;                // [warps][PS] im
-    float* str = spi + kWarps * PS;                // [16][RS] re
-    float* sti = str + kLatPerCta * RS;            // [16][RS] im
-    const int f = blockIdx.y, th0 = blockIdx.x * kLatPerCta;
+    float* spi = spr + FftShape<R>::W * PS;                // [warps][PS] im
+    float* str = spi + FftShape<R>::W * PS;                // [16][RS] re
+    float* sti = str + FftShape<R>::LAT * RS;            // [16][RS] im
+    const int f = blockIdx.y, th0 = blockIdx.x * FftShape<R>::LAT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     load_tw(tw, nullptr, gtw, nullptr, S);
     __syncthreads();
     const int la = th0 + 2 * warp;
     if (la < S) {
-        const float* ra = grid + ((size_t)f * S + la) * S;
+        const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)la * S;
         const float* rb = ra + S;
         float2 v[R];
 #pragma unroll
@@ -348,10 +455,10 @@ __global__ void __launch_bounds__(256) k_rows_fwd_w(const float* __restrict__ gr
         }
     }
     __syncthreads();
-    const int nlat = min(kLatPerCta, S - th0);
+    const int nlat = min(FftShape<R>::LAT, S - th0);
     const size_t plane = (size_t)N * B * S;
-    for (int e = threadIdx.x; e < B * kLatPerCta; e += blockDim.x) {
-        const int m = e / kLatPerCta, q = e - m * kLatPerCta;
+    for (int e = threadIdx.x; e < B * FftShape<R>::LAT; e += blockDim.x) {
+        const int m = e / FftShape<R>::LAT, q = e - m * FftShape<R>::LAT;
         if (q >= nlat) continue;
         const size_t o = ((size_t)f * B + m) * S + th0 + q;
         X[o] = str[q * RS + pad32(m)];
@@ -361,7 +468,7 @@ __global__ void __launch_bounds__(256) k_rows_fwd_w(const float* __restrict__ gr
 
 // Weighted REDFT10 per (function, seminaive order) row: C[p][f][m][k], k < B.
 template <int R>
-__global__ void __launch_bounds__(256) k_dct_fwd_w(const float* __restrict__ X, float* __restrict__ Cout, int nrows,
+__global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(const float* __restrict__ X, float* __restrict__ Cout, int nrows,
                                                    const float* __restrict__ gw, const float2* __restrict__ gtw,
                                                    const float2* __restrict__ gtwD) {
     constexpr int S = 32 * R, B = S / 2;
@@ -372,12 +479,12 @@ __global__ void __launch_bounds__(256) k_dct_fwd_w(const float* __restrict__ X, 
     float2* twD = tw + TWL;
     float* w = fsm + 2 * TWL + 2 * S;    // 2S weights (even orders, then odd)
     float* spr = w + 2 * S;
-    float* spi = spr + kWarps * PS;
+    float* spi = spr + FftShape<R>::W * PS;
     load_tw(tw, twD, gtw, gtwD, S);
     for (int q = threadIdx.x; q < 2 * S; q += blockDim.x) w[q] = gw[q];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * kWarps + warp;
+    const int row = blockIdx.x * FftShape<R>::W + warp;
     if (row >= nrows) return;
     const int m = row % B;
     if (naive_order(m)) return;
@@ -417,7 +524,7 @@ __global__ void __launch_bounds__(256) k_dct_fwd_w(const float* __restrict__ X, 
 
 // REDFT01 per (function, seminaive order) row, sin(theta) for odd m, scale: F[p][f][m][theta].
 template <int R>
-__global__ void __launch_bounds__(256) k_dct_inv_w(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
+__global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
                                                    const float* __restrict__ gsin, const float2* __restrict__ gtw,
                                                    const float2* __restrict__ gtwD, float scale) {
     constexpr int S = 32 * R, B = S / 2;
@@ -428,12 +535,12 @@ __global__ void __launch_bounds__(256) k_dct_inv_w(const float* __restrict__ Fc,
     float2* twD = tw + TWL;
     float* sn = fsm + 2 * TWL + 2 * S;
     float* spr = sn + S;
-    float* spi = spr + kWarps * PS;
+    float* spi = spr + FftShape<R>::W * PS;
     load_tw(tw, twD, gtw, gtwD, S);
     for (int q = threadIdx.x; q < S; q += blockDim.x) sn[q] = gsin[q];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * kWarps + warp;
+    const int row = blockIdx.x * FftShape<R>::W + warp;
     if (row >= nrows) return;
     const int m = row % B;
     if (naive_order(m)) return;
@@ -473,25 +580,26 @@ __global__ void __launch_bounds__(256) k_dct_inv_w(const float* __restrict__ Fc,
 
 // DFT with sign +1 over the orders for 16 latitudes (two real output rows per warp).
 template <int R>
-__global__ void __launch_bounds__(256) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
-                                                    const float2* __restrict__ gtw) {
+__global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
+                                                    const float2* __restrict__ gtw,
+                                                    const int64_t* __restrict__ gmap) {
     constexpr int S = 32 * R, B = S / 2;
     constexpr int PS = S + S / 32;
-    constexpr int TS = kLatPerCta + 1;  // padded tile row (odd)
+    constexpr int TS = FftShape<R>::LAT + 1;  // padded tile row (odd)
     constexpr int TWL = twtab_len(S);
     extern __shared__ __align__(16) float fsm[];
     float2* tw = reinterpret_cast<float2*>(fsm);
     float* tr = fsm + 2 * TWL;           // [B][TS]
     float* ti = tr + B * TS;
     float* spr = ti + B * TS;            // [warps][PS]
-    float* spi = spr + kWarps * PS;
-    const int f = blockIdx.y, th0 = blockIdx.x * kLatPerCta;
+    float* spi = spr + FftShape<R>::W * PS;
+    const int f = blockIdx.y, th0 = blockIdx.x * FftShape<R>::LAT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     load_tw(tw, nullptr, gtw, nullptr, S);
-    const int nlat = min(kLatPerCta, S - th0);
+    const int nlat = min(FftShape<R>::LAT, S - th0);
     const size_t plane = (size_t)N * B * S;
-    for (int e = threadIdx.x; e < B * kLatPerCta; e += blockDim.x) {
-        const int m = e / kLatPerCta, q = e - m * kLatPerCta;
+    for (int e = threadIdx.x; e < B * FftShape<R>::LAT; e += blockDim.x) {
+        const int m = e / FftShape<R>::LAT, q = e - m * FftShape<R>::LAT;
         const size_t o = ((size_t)f * B + m) * S + th0 + q;
         tr[m * TS + q] = (q < nlat) ? F[o] : 0.f;
         ti[m * TS + q] = (q < nlat) ? F[plane + o] : 0.f;
@@ -528,7 +636,7 @@ __global__ void __launch_bounds__(256) k_rows_inv_w(const float* __restrict__ F,
         zi[o] = v[k1].y;
     }
     __syncwarp();
-    float* ga = grid + ((size_t)f * S + th0 + a) * S;
+    float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;
     for (int k = lane; k < S; k += 32) {
         ga[k] = zr[pad32(k)];
         if (th0 + b < S) ga[S + k] = zi[pad32(k)];
@@ -555,22 +663,46 @@ __global__ void k_naive_combine(float* F, int N, int B, float scale) {
 }
 
 // ------------------------------------------------------------------------------------
-// Tensor-core Legendre contraction, one (order, 64 functions, parity, latitude block) per CTA:
-// D[128 x NP] = A[128 x K] * B[NP x K]^T, A = 64 functions x (re, im) rows in three BF16
-// terms (exact for FP32), B = the packed table blob, FP32 accumulation in TMEM.
-struct Leg {
-    const float* C;          // forward seminaive: C[p][f][m][k]
-    const float* X;          // forward naive: latitude samples X[p][f][m][theta]
-    const float* rc_in;      // inverse: coefficients
+// Tensor-core Legendre contraction.  A persistent kernel: each CTA takes work items from a
+// counter; an item is (bandwidth class, 64 functions, order m, latitude block nb, table-row
+// sub-block, parity t of l-m) and computes D[128 x NB] = A[128 x K] * B[NB x K]^T, A = 64
+// functions x (re, im) rows in split terms, B = rows [n0, n0 + NB) of the packed table blob,
+// FP32 accumulation in TMEM.  NB (the N extent of the tile) is chosen per class at launch.
+// Barriers and TMEM are set up once per CTA; the stage and phase of every chunk follow a
+// running per-CTA chunk count, so consecutive items keep the two-stage pipeline.
+//
+// FP16 terms (S2G_PREC_FP16X2): each A row is scaled by a power of two 2^e_r chosen from the
+// row's largest magnitude (|x| 2^e_r < 2^14) and the table blob by one power of two per
+// bandwidth, so that FP16's exponent range holds both; the epilogue undoes both scales.
+static constexpr int kMaxClasses = 6;  // bandwidths 16 .. 512
+
+struct LegClass {
+    int B, N, ntiles;         // bandwidth, functions, 64-function tiles
+    int NB;                   // table rows per work item (N extent of the tile)
+    int per_tile;             // work items per 64-function tile
+    const int* mstart;        // B + 1 prefix sums of the items of each order (within a tile)
+    int64_t item0;            // first work item of the class
+    float tab_inv;            // inverse of the table blob's scale
+    const float* C;           // forward seminaive input C[p][f][m][k]
+    const float* X;           // forward naive input X[p][f][m][theta]
+    const float* rc_in;       // inverse input coefficients
     const float* ic_in;
-    float* rc;               // forward output coefficients
+    float* rc;                // forward output coefficients
     float* ic;
-    float* Fc;               // inverse seminaive output Fcos[p][f][m][k]
-    float* F;                // inverse naive output (D0 | D1) in F[p][f][m][.]
+    float* Fc;                // inverse seminaive output Fcos[p][f][m][k]
+    float* F;                 // inverse naive output (D0 | D1) in F[p][f][m][.]
+    const int64_t* cmap;      // function -> element offset of its coefficients (null: f * B * B)
     const uint8_t* blob;
     const int64_t* blob_off;
+};
+
+struct Leg {
+    LegClass cls[kMaxClasses];
+    int ncls;
+    int nprod;
+    long long nitems;
+    int* counter;             // work counter, zero at launch
     int* err;
-    int B, N, nprod;
 };
 
 __constant__ int c_prod_a[6] = {0, 0, 1, 0, 1, 2};
@@ -578,20 +710,24 @@ __constant__ int c_prod_b[6] = {0, 1, 0, 2, 1, 0};
 
 static constexpr int kTPB = 256;
 static constexpr uint32_t kATile = 128u * kKC * 2u;  // bytes of one A term tile
+static constexpr uint32_t kSBO = (kKC / 8) * 128;    // byte stride of 8-row groups in a tile
 
-static size_t leg_smem(int B, bool fwd) {
+static int leg_npmax(int B, bool fwd) {
     int npmax = 16;
     for (int m = 0; m < B; ++m) npmax = std::max(npmax, geo(fwd, B, m).NP);
-    const size_t stage = 3 * (size_t)kATile + 3 * (size_t)npmax * kKC * 2;
-    return 1024 + 2 * stage;
+    return npmax;
+}
+
+__device__ __forceinline__ int64_t coef_base(const LegClass& k, int f) {
+    return k.cmap ? k.cmap[f] : (int64_t)f * k.B * k.B;
 }
 
 // 8 consecutive K entries of parity t for row r, segment seg of chunk c, as FP32.
 template <bool FWD>
-__device__ __forceinline__ void load_seg(const Leg& p, int m, bool nv, int t, int f, int part, int c, int seg,
+__device__ __forceinline__ void load_seg(const LegClass& k, int m, bool nv, int t, int f, int part, int c, int seg,
                                          float* v) {
-    const int B = p.B, S = 2 * B;
-    if (f >= p.N) {
+    const int B = k.B, S = 2 * B;
+    if (f >= k.N) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[q] = 0.f;
         return;
@@ -604,7 +740,7 @@ __device__ __forceinline__ void load_seg(const Leg& p, int m, bool nv, int t, in
             for (int q = 0; q < 8; ++q) v[q] = 0.f;
             return;
         }
-        const float* row = p.X + (((size_t)part * p.N + f) * B + m) * S;
+        const float* row = k.X + (((size_t)part * k.N + f) * B + m) * S;
         const float4 a0 = reinterpret_cast<const float4*>(row + j0)[0];
         const float4 a1 = reinterpret_cast<const float4*>(row + j0)[1];
         const float4 b0 = reinterpret_cast<const float4*>(row + S - 8 - j0)[0];
@@ -619,7 +755,7 @@ __device__ __forceinline__ void load_seg(const Leg& p, int m, bool nv, int t, in
     // 16 consecutive source entries, parity t taken: forward C[k], k = 2j + t; inverse a(l), l-m = 2i + t
     const int kb = 2 * (c * kKC + seg * 8);
     if (FWD) {
-        const float* src = p.C + (((size_t)part * p.N + f) * B + m) * B + kb;
+        const float* src = k.C + (((size_t)part * k.N + f) * B + m) * B + kb;
         if (kb < B) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -632,7 +768,7 @@ __device__ __forceinline__ void load_seg(const Leg& p, int m, bool nv, int t, in
             for (int q = 0; q < 8; ++q) v[q] = 0.f;
         }
     } else {
-        const float* src = (part ? p.ic_in : p.rc_in) + (size_t)f * B * B + index_of_harmonic_coeff(m, m, B);
+        const float* src = (part ? k.ic_in : k.rc_in) + coef_base(k, f) + index_of_harmonic_coeff(m, m, B);
         const int lim = B - m;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
@@ -643,196 +779,316 @@ __device__ __forceinline__ void load_seg(const Leg& p, int m, bool nv, int t, in
 }
 
 // A operand of one chunk, split into loads (issued early, held in registers across the
-// barrier and the MMA issue of the previous chunk) and the BF16 split + shared-memory store.
+// barrier and the MMA issue of the previous chunk) and the split + shared-memory store.
 static constexpr int kTasks = 128 * (kKC / 8) / kTPB;  // (row, 8-column segment) tasks per thread
 
 template <bool FWD>
-__device__ __forceinline__ void load_a(const Leg& p, int m, bool nv, int t, int f0, int c, float (&v)[kTasks][8]) {
+__device__ __forceinline__ void load_a(const LegClass& k, int m, bool nv, int t, int f0, int c,
+                                       float (&v)[kTasks][8], int tid) {
     constexpr int segs = kKC / 8;
 #pragma unroll
     for (int q = 0; q < kTasks; ++q) {
-        const int task = threadIdx.x + q * kTPB;
+        const int task = tid + q * kTPB;
         const int r = task / segs, seg = task - r * segs;
-        load_seg<FWD>(p, m, nv, t, f0 + (r & 63), r >> 6, c, seg, v[q]);
+        load_seg<FWD>(k, m, nv, t, f0 + (r & 63), r >> 6, c, seg, v[q]);
     }
 }
 
-__device__ __forceinline__ void store_a(uint8_t* st, const float (&v)[kTasks][8]) {
+// FP32 -> 16-bit terms: three BF16 (each the rounded residual of the previous; exact for FP32
+// data) or two FP16.
+template <bool F16>
+__device__ __forceinline__ void split_terms(float x, uint16_t& h0, uint16_t& h1, uint16_t& h2) {
+    if (F16) {
+        const __half a = __float2half_rn(x);
+        const __half b = __float2half_rn(x - __half2float(a));
+        h0 = __half_as_ushort(a);
+        h1 = __half_as_ushort(b);
+        h2 = 0;
+    } else {
+        __nv_bfloat16 a, b, c;
+        tc::split3(x, a, b, c);
+        h0 = __bfloat16_as_ushort(a);
+        h1 = __bfloat16_as_ushort(b);
+        h2 = __bfloat16_as_ushort(c);
+    }
+}
+
+template <bool F16>
+__device__ __forceinline__ void store_a(uint8_t* st, const float (&v)[kTasks][8], const float (&sc)[kTasks],
+                                        int tid) {
     constexpr int segs = kKC / 8;
 #pragma unroll
     for (int q = 0; q < kTasks; ++q) {
-        const int task = threadIdx.x + q * kTPB;
+        const int task = tid + q * kTPB;
         const int r = task / segs, seg = task - r * segs;
         uint32_t w[3][4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-            tc::split3(v[q][2 * j], a0, a1, a2);
-            tc::split3(v[q][2 * j + 1], b0, b1, b2);
-            w[0][j] = (uint32_t)__bfloat16_as_ushort(a0) | ((uint32_t)__bfloat16_as_ushort(b0) << 16);
-            w[1][j] = (uint32_t)__bfloat16_as_ushort(a1) | ((uint32_t)__bfloat16_as_ushort(b1) << 16);
-            w[2][j] = (uint32_t)__bfloat16_as_ushort(a2) | ((uint32_t)__bfloat16_as_ushort(b2) << 16);
+            uint16_t a0, a1, a2, b0, b1, b2;
+            split_terms<F16>(v[q][2 * j] * sc[q], a0, a1, a2);
+            split_terms<F16>(v[q][2 * j + 1] * sc[q], b0, b1, b2);
+            w[0][j] = (uint32_t)a0 | ((uint32_t)b0 << 16);
+            w[1][j] = (uint32_t)a1 | ((uint32_t)b1 << 16);
+            w[2][j] = (uint32_t)a2 | ((uint32_t)b2 << 16);
         }
         const uint32_t o = tc::tile_off(r, seg * 8, kKC);
 #pragma unroll
-        for (int s = 0; s < 3; ++s)
+        for (int s = 0; s < (F16 ? 2 : 3); ++s)
             *reinterpret_cast<uint4*>(st + s * kATile + o) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
     }
 }
 
 // 16 columns of the leading-product accumulator plus the matching correction columns.
-__device__ __forceinline__ void ld_sum(uint32_t taddr, int NP, bool corr, float* v) {
-    tc::tmem_ld16(taddr, v);
+__device__ __forceinline__ void ld_sum(uint32_t taddr, uint32_t corr_off, bool corr, float* v) {
     if (corr) {
         float u[16];
-        tc::tmem_ld16(taddr + NP, u);
+        tc::tmem_ld16x2(taddr, taddr + corr_off, v, u);
 #pragma unroll
         for (int q = 0; q < 16; ++q) v[q] += u[q];
+    } else {
+        tc::tmem_ld16(taddr, v);
     }
 }
 
+// Epilogue stores of one staged block: rows r (function f0 + r % 64, part r / 64) of the
+// staging tile `ep` (row stride ES floats), columns [0, w) of table-row block c0 = n0 + cb0.
+// Warps take rows, lanes take consecutive columns (coalesced; no per-element division).
 template <bool FWD>
-__global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes) {
+__device__ __forceinline__ void epi_store(const LegClass& K, int m, int t, int nb, int NP, int f0, int c0, int w,
+                                          const float* ep, int ES, int wid, int nw, int lane) {
+    const int B = K.B;
+    if (FWD) {
+        const int base = index_of_harmonic_coeff(m, m, B) + t + 2 * c0;
+        const int nbase = index_of_harmonic_coeff(-m, m, B) + t + 2 * c0;
+        const int nv_ = min(w, nr_par(B, m, t) - c0);
+        const float sgn = (m & 1) ? -1.f : 1.f;
+        for (int r = wid; r < 128; r += nw) {
+            const int f = f0 + (r & 63), part = r >> 6;
+            if (f >= K.N) continue;
+            const float* src = ep + r * ES;
+            float* out = (part ? K.ic : K.rc) + coef_base(K, f);
+            const float s2 = part ? -sgn : sgn;
+            for (int i = lane; i < nv_; i += 32) {
+                const float v = src[i];
+                out[base + 2 * i] = v;
+                if (m) out[nbase + 2 * i] = s2 * v;
+            }
+        }
+    } else if (!naive_order(m)) {
+        const float sc_ = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
+        const int nj = min(w, B / 2 - c0);
+        for (int r = wid; r < 128; r += nw) {
+            const int f = f0 + (r & 63), part = r >> 6;
+            if (f >= K.N) continue;
+            const float* src = ep + r * ES;
+            float* dst = K.Fc + (((size_t)part * K.N + f) * B + m) * B + t;
+            for (int j = lane; j < nj; j += 32) {
+                const int kk = 2 * (c0 + j);
+                dst[kk] = src[j] * ((kk + t) == 0 ? sc0 : sc_);
+            }
+        }
+    } else {
+        for (int r = wid; r < 128; r += nw) {
+            const int f = f0 + (r & 63), part = r >> 6;
+            if (f >= K.N) continue;
+            const float* src = ep + r * ES;
+            float* dst = K.F + (((size_t)part * K.N + f) * B + m) * (2 * B) + t * B + nb * NP + c0;
+            for (int i = lane; i < w; i += 32) dst[i] = src[i];
+        }
+    }
+}
+
+// Bulk copies of table rows [n0, n0 + rows) of chunk c, all terms, into stage buffer sb.
+template <bool F16>
+__device__ __forceinline__ void issue_table(uint8_t* sb, const uint8_t* blob, int NP, int n0, int rows, int c,
+                                            uint64_t* bar) {
+    constexpr int NT = F16 ? 2 : 3;
+    const uint32_t tile = (uint32_t)NP * kKC * 2, part = (uint32_t)rows * kKC * 2;
+    const uint8_t* src = blob + (size_t)c * NT * tile + (size_t)(n0 / 8) * kSBO;
+    tc::mbar_arrive_expect_tx(bar, NT * part);
+#pragma unroll
+    for (int s = 0; s < NT; ++s) tc::bulk_g2s(sb + s * part, src + (size_t)s * tile, part, bar);
+}
+
+template <bool FWD, bool F16>
+__global__ void __launch_bounds__(kTPB, 2) k_leg_tc(Leg p, uint32_t stage_bytes, uint32_t ncols) {
+    constexpr int NT = F16 ? 2 : 3;
     extern __shared__ __align__(1024) uint8_t dsm[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
     __shared__ uint64_t bars[4];  // [0,1] table bytes landed, [2,3] MMAs of the stage done
     __shared__ uint32_t tmem_slot;
     __shared__ int s_abort;
-    const int B = p.B;
-    // parity is the fastest grid index: the two CTAs that write the interleaved (stride-2)
-    // halves of the same coefficient rows run back to back, so their sectors merge in L2
-    const int t = blockIdx.x & 1, nb = blockIdx.x >> 1;
-    const int m = blockIdx.y, f0 = blockIdx.z * 64;
-    const Geo g = geo(FWD, B, m);
-    if (nb >= g.nblk) return;  // uniform per CTA, before any barrier or TMEM use
-    const bool nv = naive_order(m);
-    const int NP = g.NP, nchunks = g.nch;
-    const uint32_t bt = (uint32_t)NP * kKC * 2;
-    // two accumulators: columns [0, NP) take the leading product x0*t0, [NP, 2NP) the
-    // correction products; each FP32 accumulation step in TMEM truncates relative to the
-    // accumulator's own magnitude, so the small terms are not rounded against the large sum
-    uint32_t ncols = 32;
-    while (ncols < (uint32_t)(2 * NP)) ncols <<= 1;
+    __shared__ int s_dec[6];  // decoded item: class, m, t, sub-block, latitude block, first function
+    __shared__ float s_rinv[128];  // per-row inverse scale (FP16 terms)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint8_t* blob = p.blob + p.blob_off[m] + (size_t)(t * g.nblk + nb) * nchunks * 3 * bt;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < 4; ++i) tc::mbar_init(&bars[i], 1);
         tc::fence_mbar_init();
         s_abort = 0;
     }
+    // two accumulators per item: columns [0, NB) take the leading product x0*t0, [ncols/2,
+    // ncols/2 + NB) the correction products; each FP32 accumulation step in TMEM truncates
+    // relative to the accumulator's own magnitude, so the small terms are not rounded against
+    // the large sum
     if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    const uint32_t tmem = tmem_slot;
-    const uint32_t idesc = tc::idesc_bf16_f32(128, NP);
-    constexpr uint32_t sbo = (kKC / 8) * 128;
+    const uint32_t tmem = tmem_slot, corr = ncols / 2;
+    uint32_t gc = 0;  // chunks this CTA has processed: stage gc & 1, barrier phase (gc >> 1) & 1
+    // next work item (thread 0): fetched one item ahead, during the previous item's epilogue
+    long long item = threadIdx.x == 0 ? (long long)atomicAdd(p.counter, 1) : 0;
 
-    // Table chunks: 0 and 1 are issued here; chunk c+1 is issued right after the MMAs of chunk
-    // c, as soon as those of chunk c-1 (the previous user of that stage) have retired.
-    if (threadIdx.x == 0) {
-        for (int c = 0; c < 2 && c < nchunks; ++c) {
-            tc::mbar_arrive_expect_tx(&bars[c], 3 * bt);
-            tc::bulk_g2s(smem + c * stage_bytes + 3 * kATile, blob + (size_t)c * 3 * bt, 3 * bt, &bars[c]);
-        }
-    }
-    float va[kTasks][8];
-    load_a<FWD>(p, m, nv, t, f0, 0, va);
-    for (int c = 0; c < nchunks; ++c) {
-        const int s = c & 1;
-        uint8_t* st = smem + s * stage_bytes;
-        // the A part of stage s was last read by the MMAs of chunk c-2; thread 0 waited for them
-        // at the end of iteration c-1, before it issued the table copy of chunk c into stage s
-        __syncthreads();
-        if (s_abort) break;
-        store_a(st, va);
-        if (c + 1 < nchunks) load_a<FWD>(p, m, nv, t, f0, c + 1, va);  // in flight across the MMA issue
-        tc::fence_proxy_async_smem();
-        __syncthreads();
+    for (;;) {
+        __syncthreads();  // the previous item's epilogue has finished with shared memory
         if (threadIdx.x == 0) {
-            if (!tc::mbar_wait(&bars[s], (c >> 1) & 1)) {
-                s_abort = 1;
+            // decode: class, then (64-function tile, order m, latitude block nb, sub-block, parity t);
+            // parity is the fastest index, so the two items that write the interleaved (stride-2)
+            // halves of the same coefficient rows run back to back and their sectors merge in L2
+            if (item >= p.nitems) {
+                s_dec[0] = -1;
             } else {
-                tc::tc_fence_after();
-                const uint32_t sa = tc::smem_u32(st), sb = tc::smem_u32(st + 3 * kATile);
-                for (int ks = 0; ks < kKC / 16; ++ks) {
-                    for (int pr = 0; pr < p.nprod; ++pr) {
-                        const uint64_t da = tc::sdesc(sa + c_prod_a[pr] * kATile + ks * 256, 128, sbo);
-                        const uint64_t db = tc::sdesc(sb + c_prod_b[pr] * bt + ks * 256, 128, sbo);
-                        const bool first = (c == 0 && ks == 0 && pr <= 1);  // first write of either accumulator
-                        tc::mma_bf16(tmem + (pr ? NP : 0), da, db, idesc, first ? 0u : 1u);
-                    }
+                int ci = 0;
+                while (ci + 1 < p.ncls && item >= p.cls[ci + 1].item0) ++ci;
+                const LegClass& K = p.cls[ci];
+                const long long li = item - K.item0;
+                const int rem = (int)(li % K.per_tile);
+                int lo = 0, hi = K.B - 1;  // largest m with mstart[m] <= rem
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (K.mstart[mid] <= rem) lo = mid;
+                    else hi = mid - 1;
                 }
-                tc::mma_commit(&bars[2 + s]);
-                // stage s^1 is free once the MMAs of chunk c-1 retire: fetch chunk c+1 into it
-                if (c + 1 < nchunks && c >= 1) {
-                    if (!tc::mbar_wait(&bars[2 + (s ^ 1)], ((c - 1) >> 1) & 1)) {
-                        s_abort = 1;
-                    } else {
-                        uint8_t* sn = smem + (s ^ 1) * stage_bytes;
-                        tc::mbar_arrive_expect_tx(&bars[s ^ 1], 3 * bt);
-                        tc::bulk_g2s(sn + 3 * kATile, blob + (size_t)(c + 1) * 3 * bt, 3 * bt, &bars[s ^ 1]);
-                    }
-                }
+                const int j = rem - K.mstart[lo];
+                const int nsub = (geo(FWD, K.B, lo).NP + K.NB - 1) / K.NB;
+                s_dec[0] = ci;
+                s_dec[1] = lo;
+                s_dec[2] = j & 1;
+                s_dec[3] = (j >> 1) % nsub;
+                s_dec[4] = (j >> 1) / nsub;
+                s_dec[5] = (int)(li / K.per_tile) * 64;
             }
         }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && !s_abort) {
-        const int last = nchunks - 1;
-        if (!tc::mbar_wait(&bars[2 + (last & 1)], (last >> 1) & 1)) s_abort = 1;
-    }
-    __syncthreads();
-    // Epilogue: TMEM -> registers (warps 0-3, one accumulator row per thread) -> padded smem
-    // tile D[r][i] (stage buffers are free once the last commit has arrived) -> all 8 warps
-    // write the outputs with consecutive threads on consecutive columns.
-    float* dt = reinterpret_cast<float*>(smem);
-    const int DS = NP + 1;  // odd row stride
-    if (!s_abort && warp < 4) {
-        tc::tc_fence_after();
-        const int r = warp * 32 + lane;
-        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int cb = 0; cb < NP; cb += 16) {
-            float v[16];
-            ld_sum(trow + cb, NP, p.nprod > 1, v);
+        __syncthreads();
+        if (s_dec[0] < 0 || s_abort) break;
+        const LegClass K = p.cls[s_dec[0]];  // by value: registers, not parameter-space loads in the loops
+        const int m = s_dec[1], t = s_dec[2], sub = s_dec[3], nb = s_dec[4], f0 = s_dec[5];
+        const int B = K.B;
+        const Geo g = geo(FWD, B, m);
+        const int n0 = sub * K.NB;
+        const int rows = min(K.NB, g.NP - n0);
+        const bool nv = naive_order(m);
+        const int nchunks = g.nch;
+        const uint8_t* blob = K.blob + K.blob_off[m] + (size_t)(t * g.nblk + nb) * nchunks * NT * g.NP * kKC * 2;
+        const uint32_t idesc = F16 ? tc::idesc_f16_f32(128, rows) : tc::idesc_bf16_f32(128, rows);
+
+        // Table chunks 0 and 1 are issued here (every MMA of the previous item has retired);
+        // chunk c+1 right after the MMAs of chunk c, once those of chunk c-1 have retired.
+        if (threadIdx.x == 0) {
+            for (int c = 0; c < 2 && c < nchunks; ++c) {
+                const uint32_t s = (gc + c) & 1;
+                issue_table<F16>(smem + s * stage_bytes + NT * kATile, blob, g.NP, n0, rows, c, &bars[s]);
+            }
+        }
+        float va[kTasks][8];
+        float sc[kTasks];
+        if (F16) {
+            // row scales: largest magnitude of each row over all chunks; the pass runs from the
+            // last chunk down, so chunk 0 is left in registers for the main loop
+            float mx[kTasks];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) dt[r * DS + cb + q] = v[q];
-        }
-    }
-    __syncthreads();
-    if (!s_abort) {
-        if (FWD) {
-            const int base = index_of_harmonic_coeff(m, m, B) + t;
-            const int nbase = index_of_harmonic_coeff(-m, m, B) + t;
-            const int nv_ = (B - m - t + 1) / 2;  // degrees of this parity
-            for (int e = threadIdx.x; e < 128 * nv_; e += kTPB) {
-                const int r = e / nv_, i = e - r * nv_;
-                const int f = f0 + (r & 63), part = r >> 6;
-                if (f >= p.N) continue;
-                const float v = dt[r * DS + i];
-                float* out = (part ? p.ic : p.rc) + (size_t)f * B * B;
-                out[base + 2 * i] = v;
-                if (m) out[nbase + 2 * i] = (((m & 1) ? -1.f : 1.f) * (part ? -1.f : 1.f)) * v;
+            for (int q = 0; q < kTasks; ++q) mx[q] = 0.f;
+            for (int c = nchunks - 1; c >= 0; --c) {
+                load_a<FWD>(K, m, nv, t, f0, c, va, threadIdx.x);
+#pragma unroll
+                for (int q = 0; q < kTasks; ++q)
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) mx[q] = fmaxf(mx[q], fabsf(va[q][e]));
             }
-        } else if (!nv) {
-            const float sc = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
-            const int nj = B / 2;
-            for (int e = threadIdx.x; e < 128 * nj; e += kTPB) {
-                const int r = e / nj, j = e - r * nj;
-                const int f = f0 + (r & 63), part = r >> 6;
-                if (f >= p.N) continue;
-                const int k = 2 * j + t;
-                p.Fc[(((size_t)part * p.N + f) * B + m) * B + k] = dt[r * DS + j] * (k == 0 ? sc0 : sc);
+#pragma unroll
+            for (int q = 0; q < kTasks; ++q) {
+                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 1));
+                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 2));
+                int e = 0;
+                frexpf(mx[q], &e);  // mx < 2^e
+                const int sh = mx[q] > 0.f ? min(14 - e, 120) : 0;
+                sc[q] = ldexpf(1.f, sh);
+                const int task = threadIdx.x + q * kTPB;
+                if ((task & 3) == 0) s_rinv[task >> 2] = ldexpf(1.f, -sh);
             }
         } else {
-            for (int e = threadIdx.x; e < 128 * NP; e += kTPB) {
-                const int r = e / NP, i = e - r * NP;
-                const int f = f0 + (r & 63), part = r >> 6;
-                if (f >= p.N) continue;
-                p.F[(((size_t)part * p.N + f) * B + m) * (2 * B) + t * B + nb * NP + i] = dt[r * DS + i];
+#pragma unroll
+            for (int q = 0; q < kTasks; ++q) sc[q] = 1.f;
+            load_a<FWD>(K, m, nv, t, f0, 0, va, threadIdx.x);
+        }
+        for (int c = 0; c < nchunks; ++c) {
+            const uint32_t gcc = gc + c;
+            const uint32_t s = gcc & 1;
+            uint8_t* st = smem + s * stage_bytes;
+            // the A part of stage s was last read by the MMAs of chunk gcc-2, which have retired
+            __syncthreads();
+            if (s_abort) break;
+            store_a<F16>(st, va, sc, threadIdx.x);
+            if (c + 1 < nchunks) load_a<FWD>(K, m, nv, t, f0, c + 1, va, threadIdx.x);  // in flight across the MMA issue
+            tc::fence_proxy_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (!tc::mbar_wait(&bars[s], (gcc >> 1) & 1)) {
+                    s_abort = 1;
+                } else {
+                    tc::tc_fence_after();
+                    const uint32_t sa = tc::smem_u32(st), sb = tc::smem_u32(st + NT * kATile);
+                    const uint32_t bpart = (uint32_t)rows * kKC * 2;
+                    for (int ks = 0; ks < kKC / 16; ++ks) {
+                        for (int pr = 0; pr < p.nprod; ++pr) {
+                            const uint64_t da = tc::sdesc(sa + c_prod_a[pr] * kATile + ks * 256, 128, kSBO);
+                            const uint64_t db = tc::sdesc(sb + c_prod_b[pr] * bpart + ks * 256, 128, kSBO);
+                            const bool first = (c == 0 && ks == 0 && pr <= 1);  // first write of an accumulator
+                            tc::mma_bf16(tmem + (pr ? corr : 0u), da, db, idesc, first ? 0u : 1u);
+                        }
+                    }
+                    tc::mma_commit(&bars[2 + s]);
+                    if (c + 1 < nchunks && c >= 1) {
+                        if (!tc::mbar_wait(&bars[2 + (s ^ 1)], ((gcc - 1) >> 1) & 1)) {
+                            s_abort = 1;
+                        } else {
+                            uint8_t* sn = smem + (s ^ 1) * stage_bytes + NT * kATile;
+                            issue_table<F16>(sn, blob, g.NP, n0, rows, c + 1, &bars[s ^ 1]);
+                        }
+                    }
+                }
             }
         }
+        __syncthreads();
+        if (threadIdx.x == 0 && !s_abort) {
+            const uint32_t gl = gc + nchunks - 1;
+            if (!tc::mbar_wait(&bars[2 + (gl & 1)], (gl >> 1) & 1)) s_abort = 1;
+        }
+        gc += nchunks;
+        if (threadIdx.x == 0) item = atomicAdd(p.counter, 1);  // overlaps the epilogue
+        __syncthreads();
+        if (s_abort) break;
+        // Epilogue: TMEM -> registers (warps 0-3, one accumulator row per thread) -> padded smem
+        // tile D[r][i] (the stage buffers are free: all copies and MMAs of this item are done)
+        // -> all 8 warps write the outputs with consecutive threads on consecutive columns.
+        float* dt = reinterpret_cast<float*>(smem);
+        const int DS = rows + 1;  // odd row stride
+        if (warp < 4) {
+            tc::tc_fence_after();
+            const int r = warp * 32 + lane;
+            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+            const float rs = F16 ? s_rinv[r] * K.tab_inv : 1.f;
+            for (int cb = 0; cb < rows; cb += 16) {
+                float v[16];
+                ld_sum(trow + cb, corr, p.nprod > 1, v);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) dt[r * DS + cb + q] = v[q] * rs;
+            }
+            tc::tc_fence_before();
+        }
+        __syncthreads();
+        epi_store<FWD>(K, m, t, nb, g.NP, f0, n0, rows, dt, DS, warp, kTPB / 32, lane);
     }
     if (s_abort && threadIdx.x == 0) atomicExch(p.err, S2G_ERR_TIMEOUT);
     tc::tc_fence_before();
@@ -844,41 +1100,495 @@ __global__ void __launch_bounds__(kTPB, 1) k_leg_tc(Leg p, uint32_t stage_bytes)
 }
 
 // ------------------------------------------------------------------------------------
+// Warp-specialised form of the contraction: the same work items and the same arithmetic per
+// item as k_leg_tc (results are bit-identical), with the stages of consecutive items
+// overlapped.  16 warps, one CTA per SM:
+//   warp 0     : scheduler (fetches and decodes items into a kNI-entry ring in shared memory)
+//                and table producer (bulk copies into an nbs-stage ring);
+//   warp 1     : MMA issuer (one thread; two accumulator pairs in TMEM when they fit, so the
+//                epilogue of item k overlaps the MMAs of item k+1);
+//   warps 4-7  : epilogue (warp 4+q reads TMEM lanes 32q..32q+31 = accumulator rows, stages
+//                128-column blocks in shared memory, writes them coalesced);
+//   warps 8-15 : A producers (FP32 loads one chunk ahead, split, store into a kNAS-stage ring);
+//   warps 2-3  : no role.
+// Every mbarrier wait is bounded; on expiry the role records the abort and leaves its loop,
+// the table producer waits (bounded) for its copies in flight, the MMA thread for its MMAs,
+// and the CTA frees TMEM and returns.
+static constexpr int kWsThreads = 512;
+static constexpr int kNI = 4;          // item ring entries
+static constexpr int kNAS = 2;         // A stages
+static constexpr int kMaxNBS = 8;      // table stages (upper bound)
+static constexpr int kEpiCols = 128;   // epilogue staging width
+static constexpr int kAProd = 256;     // A-producer threads
+static constexpr int kEpi = 128;       // epilogue threads
+
+struct WsItem {
+    int ci, m, t, sub, nb, f0;
+};
+
+template <bool FWD>
+__device__ __forceinline__ WsItem decode_item(const Leg& p, long long item) {
+    WsItem e;
+    if (item >= p.nitems) {
+        e.ci = -1;
+        return e;
+    }
+    int ci = 0;
+    while (ci + 1 < p.ncls && item >= p.cls[ci + 1].item0) ++ci;
+    const LegClass& K = p.cls[ci];
+    const long long li = item - K.item0;
+    const int rem = (int)(li % K.per_tile);
+    int lo = 0, hi = K.B - 1;  // largest m with mstart[m] <= rem
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (K.mstart[mid] <= rem) lo = mid;
+        else hi = mid - 1;
+    }
+    const int j = rem - K.mstart[lo];
+    const int nsub = (geo(FWD, K.B, lo).NP + K.NB - 1) / K.NB;
+    e.ci = ci;
+    e.m = lo;
+    e.t = j & 1;
+    e.sub = (j >> 1) % nsub;
+    e.nb = (j >> 1) / nsub;
+    e.f0 = (int)(li / K.per_tile) * 64;
+    return e;
+}
+
+template <bool FWD, bool F16>
+__global__ void __launch_bounds__(kWsThreads, 1)
+    k_leg_ws(Leg p, uint32_t b_off, uint32_t b_stage, int nbs, uint32_t epi_off, uint32_t ncols, int nacc) {
+    constexpr int NT = F16 ? 2 : 3;
+    constexpr uint32_t kAStage = NT * kATile;
+    extern __shared__ __align__(1024) uint8_t dsm[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t item_full[kNI], item_empty[kNI], sc_full[kNI];
+    __shared__ uint64_t a_full[kNAS], a_empty[kNAS], b_full[kMaxNBS], b_empty[kMaxNBS];
+    __shared__ uint64_t acc_full[2], acc_empty[2], fin;
+    __shared__ WsItem items[kNI];
+    __shared__ float s_rinv[kNI][128];
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int s_abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kNI; ++i) {
+            tc::mbar_init(&item_full[i], 1);
+            tc::mbar_init(&item_empty[i], 1 + kAProd + kEpi);
+            tc::mbar_init(&sc_full[i], kAProd);
+        }
+        for (int i = 0; i < kNAS; ++i) {
+            tc::mbar_init(&a_full[i], kAProd);
+            tc::mbar_init(&a_empty[i], 1);
+        }
+        for (int i = 0; i < nbs; ++i) {
+            tc::mbar_init(&b_full[i], 1);
+            tc::mbar_init(&b_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&acc_full[i], 1);
+            tc::mbar_init(&acc_empty[i], kEpi);
+        }
+        tc::mbar_init(&fin, 1);
+        tc::fence_mbar_init();
+        s_abort = 0;
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t accw = ncols / nacc;  // columns of one accumulator pair
+    const uint32_t corr = accw / 2;      // offset of the correction accumulator
+
+    if (warp == 0) {
+        // ---------------- scheduler + table producer ----------------
+        if (lane == 0) {
+            uint32_t bc = 0;  // table chunks issued
+            for (int k = 0; !s_abort; ++k) {
+                const int slot = k % kNI;
+                if (!tc::mbar_wait(&item_empty[slot], ((k / kNI) & 1) ^ 1)) {
+                    s_abort = 1;
+                    break;
+                }
+                const WsItem e = decode_item<FWD>(p, atomicAdd(p.counter, 1));
+                items[slot] = e;
+                tc::mbar_arrive(&item_full[slot]);
+                if (e.ci < 0) break;
+                const LegClass& K = p.cls[e.ci];
+                const Geo g = geo(FWD, K.B, e.m);
+                const int n0 = e.sub * K.NB, rows = min(K.NB, g.NP - n0);
+                const uint8_t* blob =
+                    K.blob + K.blob_off[e.m] + (size_t)(e.t * g.nblk + e.nb) * g.nch * NT * g.NP * kKC * 2;
+                for (int c = 0; c < g.nch; ++c, ++bc) {
+                    const int s = bc % nbs;
+                    if (!tc::mbar_wait(&b_empty[s], ((bc / nbs) & 1) ^ 1)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    issue_table<F16>(smem + b_off + s * b_stage, blob, g.NP, n0, rows, c, &b_full[s]);
+                }
+            }
+            // copies in flight land before the CTA leaves (immediate on the normal path)
+            for (uint32_t j = bc > (uint32_t)nbs ? bc - nbs : 0; j < bc; ++j)
+                tc::mbar_wait(&b_full[j % nbs], (j / nbs) & 1);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t ac = 0, bc = 0;
+            for (int k = 0; !s_abort; ++k) {
+                const int slot = k % kNI;
+                if (!tc::mbar_wait(&item_full[slot], (k / kNI) & 1)) {
+                    s_abort = 1;
+                    break;
+                }
+                const WsItem e = items[slot];
+                tc::mbar_arrive(&item_empty[slot]);
+                if (e.ci < 0) break;
+                const LegClass& K = p.cls[e.ci];
+                const Geo g = geo(FWD, K.B, e.m);
+                const int rows = min(K.NB, g.NP - e.sub * K.NB);
+                const uint32_t idesc = F16 ? tc::idesc_f16_f32(128, rows) : tc::idesc_bf16_f32(128, rows);
+                const uint32_t bpart = (uint32_t)rows * kKC * 2;
+                const int buf = k % nacc;
+                if (!tc::mbar_wait(&acc_empty[buf], ((k / nacc) & 1) ^ 1)) {
+                    s_abort = 1;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t d0 = tmem + buf * accw;
+                bool ok = true;
+                for (int c = 0; c < g.nch; ++c, ++ac, ++bc) {
+                    const int sa = ac % kNAS, sb = bc % nbs;
+                    if (!tc::mbar_wait(&a_full[sa], (ac / kNAS) & 1) || !tc::mbar_wait(&b_full[sb], (bc / nbs) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t sa_addr = tc::smem_u32(smem + sa * kAStage);
+                    const uint32_t sb_addr = tc::smem_u32(smem + b_off + sb * b_stage);
+                    for (int ks = 0; ks < kKC / 16; ++ks) {
+                        for (int pr = 0; pr < p.nprod; ++pr) {
+                            const uint64_t da = tc::sdesc(sa_addr + c_prod_a[pr] * kATile + ks * 256, 128, kSBO);
+                            const uint64_t db = tc::sdesc(sb_addr + c_prod_b[pr] * bpart + ks * 256, 128, kSBO);
+                            const bool first = (c == 0 && ks == 0 && pr <= 1);
+                            tc::mma_bf16(d0 + (pr ? corr : 0u), da, db, idesc, first ? 0u : 1u);
+                        }
+                    }
+                    tc::mma_commit(&a_empty[sa]);
+                    tc::mma_commit(&b_empty[sb]);
+                }
+                if (!ok) {
+                    s_abort = 1;
+                    break;
+                }
+                tc::mma_commit(&acc_full[buf]);
+            }
+            // every MMA issued has completed before TMEM is freed
+            tc::mma_commit(&fin);
+            tc::mbar_wait(&fin, 0);
+        }
+    } else if (warp >= 4 && warp < 8) {
+        // ---------------- epilogue ----------------
+        const int et = threadIdx.x - 128;  // accumulator row = TMEM lane
+        float* ep = reinterpret_cast<float*>(smem + epi_off);
+        constexpr int ES = kEpiCols + 1;   // odd row stride
+        for (int k = 0;; ++k) {
+            const int slot = k % kNI;
+            const int buf = k % nacc;
+            bool ok = tc::mbar_wait(&item_full[slot], (k / kNI) & 1);
+            WsItem e = items[slot];
+            if (ok && e.ci >= 0) {
+                ok = tc::mbar_wait(&acc_full[buf], (k / nacc) & 1);
+                if (ok && F16) ok = tc::mbar_wait(&sc_full[slot], (k / kNI) & 1);
+            }
+            // the 128 epilogue threads take every decision below together (they share named barriers)
+            if (!tc::named_bar_and(1, kEpi, ok && !s_abort)) {
+                s_abort = 1;
+                break;
+            }
+            if (e.ci < 0) {
+                tc::mbar_arrive(&item_empty[slot]);
+                break;
+            }
+            const LegClass K = p.cls[e.ci];
+            const int B = K.B, m = e.m, t = e.t;
+            const Geo g = geo(FWD, B, m);
+            const int n0 = e.sub * K.NB, rows = min(K.NB, g.NP - n0);
+            const float rs = F16 ? s_rinv[slot][et] * K.tab_inv : 1.f;
+            tc::tc_fence_after();
+            const uint32_t trow = tmem + buf * accw + ((uint32_t)((warp & 3) * 32) << 16);
+            for (int cb0 = 0; cb0 < rows; cb0 += kEpiCols) {
+                const int w = min(kEpiCols, rows - cb0);
+                for (int cb = 0; cb < w; cb += 16) {
+                    float v[16];
+                    ld_sum(trow + cb0 + cb, corr, p.nprod > 1, v);
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) ep[et * ES + cb + q] = v[q] * rs;
+                }
+                if (cb0 + kEpiCols >= rows) {  // last TMEM read of this item: release the buffer
+                    tc::tc_fence_before();
+                    tc::mbar_arrive(&acc_empty[buf]);
+                }
+                tc::named_bar_sync(1, kEpi);
+                epi_store<FWD>(K, m, t, e.nb, g.NP, e.f0, n0 + cb0, w, ep, ES, warp - 4, 4, lane);
+                tc::named_bar_sync(1, kEpi);
+            }
+            tc::mbar_arrive(&item_empty[slot]);
+        }
+    } else if (warp >= 8) {
+        // ---------------- A producers ----------------
+        const int tid = threadIdx.x - 256;
+        uint32_t ac = 0;
+        float va[kTasks][8];
+        float sc[kTasks];
+        for (int k = 0; !s_abort; ++k) {
+            const int slot = k % kNI;
+            // warp-uniform: the F16 row scales below use full-warp shuffles
+            if (!__all_sync(0xffffffffu, tc::mbar_wait(&item_full[slot], (k / kNI) & 1))) {
+                s_abort = 1;
+                break;
+            }
+            const WsItem e = items[slot];
+            tc::mbar_arrive(&item_empty[slot]);
+            if (e.ci < 0) break;
+            const LegClass K = p.cls[e.ci];
+            const int m = e.m, t = e.t, f0 = e.f0;
+            const Geo g = geo(FWD, K.B, m);
+            const bool nv = naive_order(m);
+            if (F16) {
+                float mx[kTasks];
+#pragma unroll
+                for (int q = 0; q < kTasks; ++q) mx[q] = 0.f;
+                for (int c = g.nch - 1; c >= 0; --c) {
+                    load_a<FWD>(K, m, nv, t, f0, c, va, tid);
+#pragma unroll
+                    for (int q = 0; q < kTasks; ++q)
+#pragma unroll
+                        for (int x = 0; x < 8; ++x) mx[q] = fmaxf(mx[q], fabsf(va[q][x]));
+                }
+#pragma unroll
+                for (int q = 0; q < kTasks; ++q) {
+                    mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 1));
+                    mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 2));
+                    int ex = 0;
+                    frexpf(mx[q], &ex);  // mx < 2^ex
+                    const int sh = mx[q] > 0.f ? min(14 - ex, 120) : 0;
+                    sc[q] = ldexpf(1.f, sh);
+                    const int task = tid + q * kTPB;
+                    if ((task & 3) == 0) s_rinv[slot][task >> 2] = ldexpf(1.f, -sh);
+                }
+                tc::mbar_arrive(&sc_full[slot]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < kTasks; ++q) sc[q] = 1.f;
+                load_a<FWD>(K, m, nv, t, f0, 0, va, tid);
+            }
+            bool ok = true;
+            for (int c = 0; c < g.nch; ++c, ++ac) {
+                const int s = ac % kNAS;
+                if (!tc::mbar_wait(&a_empty[s], ((ac / kNAS) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                store_a<F16>(smem + s * kAStage, va, sc, tid);
+                tc::fence_proxy_async_smem();
+                tc::mbar_arrive(&a_full[s]);
+                if (c + 1 < g.nch) load_a<FWD>(K, m, nv, t, f0, c + 1, va, tid);
+            }
+            if (!ok) {
+                s_abort = 1;
+                break;
+            }
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, ncols);
+    }
+    if (threadIdx.x == 0 && s_abort) atomicExch(p.err, S2G_ERR_TIMEOUT);
+}
+
+// ------------------------------------------------------------------------------------
 size_t split_work_bytes(int bw, int batch) {
     const size_t B = bw, S = 2 * B;
     return 2 * (size_t)batch * B * (S + B) * sizeof(float) + 1024;
 }
 
 static int set_smem(const void* fn, size_t bytes) {
-    if (bytes > 48 * 1024) S2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    // always set: the 48 KiB default covers static plus dynamic shared memory
+    S2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return S2G_OK;
 }
 
-static int check_prec(int precision, int* nprod) {
+static int check_prec(int precision, int* nprod, bool* f16) {
+    *f16 = false;
     if (precision == S2G_PREC_BF16X3) *nprod = 6;
     else if (precision == S2G_PREC_BF16X2) *nprod = 3;
-    else return fail(S2G_ERR_ARG, "precision %d is not a split-BF16 mode", precision);
+    else if (precision == S2G_PREC_FP16X2) *nprod = 3, *f16 = true;
+    else return fail(S2G_ERR_ARG, "precision %d is not a split (tensor-core) mode", precision);
     return S2G_OK;
 }
 
-static int launch_leg(bool fwd, Leg& p, cudaStream_t st) {
-    const size_t smem = leg_smem(p.B, fwd);
-    const uint32_t stage = (uint32_t)((smem - 1024) / 2);
-    const void* fn = fwd ? (const void*)k_leg_tc<true> : (const void*)k_leg_tc<false>;
+// Resident CTAs per SM of a contraction kernel at a shared-memory size (cached).
+static int leg_occupancy(const void* fn, size_t smem, int* occ) {
+    static std::mutex mu;
+    static std::vector<std::pair<std::pair<const void*, size_t>, int>> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& e : cache)
+        if (e.first.first == fn && e.first.second == smem) return (*occ = e.second), S2G_OK;
+    int v = 0;
+    S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, fn, kTPB, smem));
+    cache.push_back({{fn, smem}, v});
+    *occ = v;
+    return S2G_OK;
+}
+
+// Contraction kernel: 0 = k_leg_tc (all threads load, split and stage each chunk; two CTAs
+// per SM), 1 = k_leg_ws (warp-specialised, one CTA per SM).
+static std::atomic<int> g_leg_kernel{1};
+
+static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items, int* counter, cudaStream_t st) {
+    const void* fn = fwd ? (f16 ? (const void*)k_leg_ws<true, true> : (const void*)k_leg_ws<true, false>)
+                         : (f16 ? (const void*)k_leg_ws<false, true> : (const void*)k_leg_ws<false, false>);
+    const int nt = f16 ? 2 : 3;
+    uint32_t pair = 32;
+    while (pair < 2u * nbmax) pair <<= 1;
+    const int nacc = 2 * pair <= 512 ? 2 : 1;
+    const uint32_t ncols = pair * nacc;
+    const size_t a_bytes = (size_t)kNAS * nt * kATile;
+    const size_t b_stage = (size_t)nt * nbmax * kKC * 2;
+    const size_t epi = (size_t)128 * (kEpiCols + 1) * sizeof(float);
+    int dev = 0, optin = 0, nsm = 0;
+    S2G_CUDA(cudaGetDevice(&dev));
+    S2G_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    cudaFuncAttributes fa{};
+    S2G_CUDA(cudaFuncGetAttributes(&fa, fn));
+    const long long budget = (long long)optin - (long long)fa.sharedSizeBytes - 1024;
+    const long long nbs_fit = (budget - (long long)a_bytes - (long long)epi) / (long long)b_stage;
+    const int nbs = (int)std::min<long long>(kMaxNBS, nbs_fit);
+    if (nbs < 2) return fail(S2G_ERR_UNSUPPORTED, "warp-specialised contraction does not fit in shared memory");
+    const size_t smem = 1024 + a_bytes + (size_t)nbs * b_stage + epi;
     S2G_TRY(set_smem(fn, smem));
-    int nblk = 1;
-    for (int m = 0; m < p.B; ++m) nblk = std::max(nblk, geo(fwd, p.B, m).nblk);
-    dim3 grid(2 * nblk, p.B, (p.N + 63) / 64);
-    if (fwd)
-        {
-            ProfScope ps_("leg_tc_fwd", st);
-            k_leg_tc<true><<<grid, kTPB, smem, st>>>(p, stage);
-        }
-    else
-        {
-            ProfScope ps_("leg_tc_inv", st);
-            k_leg_tc<false><<<grid, kTPB, smem, st>>>(p, stage);
-        }
+    const int grid = (int)std::min<long long>(items, nsm);
+    S2G_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+    const uint32_t b_off = (uint32_t)a_bytes, epi_off = (uint32_t)(a_bytes + nbs * b_stage);
+    {
+        ProfScope ps_(fwd ? "leg_tc_fwd" : "leg_tc_inv", st);
+        if (fwd && f16)
+            k_leg_ws<true, true><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols, nacc);
+        else if (fwd)
+            k_leg_ws<true, false><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols, nacc);
+        else if (f16)
+            k_leg_ws<false, true><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols, nacc);
+        else
+            k_leg_ws<false, false><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols,
+                                                                   nacc);
+    }
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+// Device table of the work items of each order for tile N extent NB: order m has
+// 2 (parities) x nblk(m) (latitude blocks) x ceil(NP(m) / NB) (sub-blocks) items.
+static int get_mstart(Split* s, bool fwd, int NB, const int** out, int* per_tile) {
+    std::lock_guard<std::mutex> lk(g_split_mu);
+    const int B = s->B;
+    std::vector<int> h(B + 1, 0);
+    for (int m = 0; m < B; ++m) {
+        const Geo g = geo(fwd, B, m);
+        h[m + 1] = h[m] + 2 * g.nblk * ((g.NP + NB - 1) / NB);
+    }
+    *per_tile = h[B];
+    for (auto& e : s->mstart[fwd])
+        if (e.first == NB) return (*out = e.second), S2G_OK;
+    int* d = nullptr;
+    S2G_CUDA(cudaMalloc(&d, sizeof(int) * (B + 1)));
+    const cudaError_t e = cudaMemcpy(d, h.data(), sizeof(int) * (B + 1), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "cudaMemcpy");
+    }
+    s->mstart[fwd].push_back({NB, d});
+    *out = d;
+    return S2G_OK;
+}
+
+int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* counter, int ctas_per_sm,
+              cudaStream_t st) {
+    int nprod;
+    bool f16;
+    S2G_TRY(check_prec(precision, &nprod, &f16));
+    if (ncls < 1 || ncls > kMaxClasses) return fail(S2G_ERR_ARG, "%d bandwidth classes (1..%d)", ncls, kMaxClasses);
+    Leg p{};
+    p.ncls = ncls;
+    p.nprod = nprod;
+    p.counter = counter;
+    long long items = 0;
+    int nbmax = 16;
+    for (int c = 0; c < ncls; ++c) {
+        const LegSpec& q = spec[c];
+        S2G_TRY(f16 ? build_split16(q.t) : build_split(q.t));
+        Split* s = (Split*)q.t->split;
+        LegClass& k = p.cls[c];
+        const int B = q.t->bw, npmax = leg_npmax(B, fwd);
+        int NB = q.NB > 0 ? std::min(q.NB, npmax) : npmax;
+        NB = std::max(16, std::min(256, NB) & ~15);  // the MMA's N is at most 256
+        k.B = B;
+        k.N = q.N;
+        k.ntiles = (q.N + 63) / 64;
+        k.NB = NB;
+        S2G_TRY(get_mstart(s, fwd, NB, &k.mstart, &k.per_tile));
+        k.item0 = items;
+        k.tab_inv = f16 ? (float)(1.0 / s->tab16) : 1.f;
+        k.C = q.C;
+        k.X = q.X;
+        k.rc_in = q.rc_in;
+        k.ic_in = q.ic_in;
+        k.rc = q.rc;
+        k.ic = q.ic;
+        k.Fc = q.Fc;
+        k.F = q.F;
+        k.cmap = q.cmap;
+        k.blob = fwd ? (f16 ? s->fwd16 : s->fwd_blob) : (f16 ? s->inv16 : s->inv_blob);
+        k.blob_off = fwd ? (f16 ? s->fwd16_off : s->fwd_off) : (f16 ? s->inv16_off : s->inv_off);
+        if (c == 0) p.err = s->err;
+        items += (long long)k.ntiles * k.per_tile;
+        nbmax = std::max(nbmax, NB);
+    }
+    p.nitems = items;
+    if (items == 0) return S2G_OK;
+    if (items > 0x7fffffffLL) return fail(S2G_ERR_ARG, "contraction of %lld work items is too large", items);
+    const int nt = f16 ? 2 : 3;
+    if (g_leg_kernel == 1) return launch_leg_ws(fwd, f16, p, nbmax, items, counter, st);
+    const size_t stage = (size_t)nt * kATile + (size_t)nt * nbmax * kKC * 2;
+    const size_t epi = (size_t)128 * (nbmax + 1) * sizeof(float);
+    const size_t smem = 1024 + std::max(2 * stage, epi);
+    uint32_t ncols = 32;
+    while (ncols < 2u * nbmax) ncols <<= 1;
+    const void* fn = fwd ? (f16 ? (const void*)k_leg_tc<true, true> : (const void*)k_leg_tc<true, false>)
+                         : (f16 ? (const void*)k_leg_tc<false, true> : (const void*)k_leg_tc<false, false>);
+    S2G_TRY(set_smem(fn, smem));
+    int occ = 0, dev = 0, nsm = 0;
+    S2G_TRY(leg_occupancy(fn, smem, &occ));
+    S2G_CUDA(cudaGetDevice(&dev));
+    S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    occ = std::min(occ, (int)(512 / ncols));  // every resident CTA holds its TMEM columns
+    if (ctas_per_sm > 0) occ = std::min(occ, ctas_per_sm);
+    if (occ < 1) return fail(S2G_ERR_UNSUPPORTED, "contraction kernel does not fit on an SM (%zu B smem)", smem);
+    const int grid = (int)std::min<long long>(items, (long long)occ * nsm);
+    S2G_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+    {
+        ProfScope ps_(fwd ? "leg_tc_fwd" : "leg_tc_inv", st);
+        if (fwd && f16) k_leg_tc<true, true><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
+        else if (fwd) k_leg_tc<true, false><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
+        else if (f16) k_leg_tc<false, true><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
+        else k_leg_tc<false, false><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
+    }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
@@ -886,9 +1596,10 @@ static int launch_leg(bool fwd, Leg& p, cudaStream_t st) {
 // ---- warp-FFT kernel launchers (dispatch on R = S / 32) ----
 template <int R>
 static int launch_fft_kernels(int which, const void* in, void* out, int N, const Split* s, cudaStream_t st,
-                              float scale) {
+                              float scale, const int64_t* gmap) {
     constexpr int S = 32 * R, B = S / 2;
     constexpr int PS = S + S / 32;
+    constexpr int kWarps = FftShape<R>::W, kLatPerCta = FftShape<R>::LAT, kThreads = FftShape<R>::T;
     const int nrows = N * B;
     size_t smem = 0;
     if (which == 0) {  // rows forward
@@ -896,47 +1607,55 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
         S2G_TRY(set_smem((const void*)k_rows_fwd_w<R>, smem));
         dim3 g((S + kLatPerCta - 1) / kLatPerCta, N);
         ProfScope ps_("rows_fwd_f32", st);
-        k_rows_fwd_w<R><<<g, 256, smem, st>>>((const float*)in, (float*)out, N, scale, s->twS);
+        k_rows_fwd_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, N, scale, s->twS, gmap);
     } else if (which == 1) {  // DCT-II
         smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + 2 * S + 2 * kWarps * PS);
         S2G_TRY(set_smem((const void*)k_dct_fwd_w<R>, smem));
         ProfScope ps_("dct_fwd_f32", st);
-        k_dct_fwd_w<R><<<(nrows + kWarps - 1) / kWarps, 256, smem, st>>>((const float*)in, (float*)out, nrows, s->w32,
+        k_dct_fwd_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((const float*)in, (float*)out, nrows, s->w32,
                                                                         s->twS, s->twD);
     } else if (which == 2) {  // DCT-III
         smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + S + 2 * kWarps * PS);
         S2G_TRY(set_smem((const void*)k_dct_inv_w<R>, smem));
         ProfScope ps_("dct_inv_f32", st);
-        k_dct_inv_w<R><<<(nrows + kWarps - 1) / kWarps, 256, smem, st>>>((const float*)in, (float*)out, nrows,
+        k_dct_inv_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((const float*)in, (float*)out, nrows,
                                                                         s->sin32, s->twS, s->twD, scale);
     } else {  // rows inverse
         smem = sizeof(float) * (2 * twtab_len(S) + 2 * B * (kLatPerCta + 1) + 2 * kWarps * PS);
         S2G_TRY(set_smem((const void*)k_rows_inv_w<R>, smem));
         dim3 g((S + kLatPerCta - 1) / kLatPerCta, N);
         ProfScope ps_("rows_inv_f32", st);
-        k_rows_inv_w<R><<<g, 256, smem, st>>>((const float*)in, (float*)out, N, s->twS);
+        k_rows_inv_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, N, s->twS, gmap);
     }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
 
 static int fft_kernels(int which, int B, const void* in, void* out, int N, const Split* s, cudaStream_t st,
-                       float scale) {
+                       float scale, const int64_t* gmap = nullptr) {
     switch (2 * B / 32) {
-        case 1: return launch_fft_kernels<1>(which, in, out, N, s, st, scale);
-        case 2: return launch_fft_kernels<2>(which, in, out, N, s, st, scale);
-        case 4: return launch_fft_kernels<4>(which, in, out, N, s, st, scale);
-        case 8: return launch_fft_kernels<8>(which, in, out, N, s, st, scale);
-        case 16: return launch_fft_kernels<16>(which, in, out, N, s, st, scale);
-        case 32: return launch_fft_kernels<32>(which, in, out, N, s, st, scale);
+        case 1: return launch_fft_kernels<1>(which, in, out, N, s, st, scale, gmap);
+        case 2: return launch_fft_kernels<2>(which, in, out, N, s, st, scale, gmap);
+        case 4: return launch_fft_kernels<4>(which, in, out, N, s, st, scale, gmap);
+        case 8: return launch_fft_kernels<8>(which, in, out, N, s, st, scale, gmap);
+        case 16: return launch_fft_kernels<16>(which, in, out, N, s, st, scale, gmap);
+        case 32: return launch_fft_kernels<32>(which, in, out, N, s, st, scale, gmap);
+        case 64: return launch_fft_kernels<64>(which, in, out, N, s, st, scale, gmap);
         default: return fail(S2G_ERR_UNSUPPORTED, "no warp FFT for bandwidth %d", B);
     }
+}
+
+// Work counter of the contraction kernel: the int after the two intermediate arrays.
+static int* work_counter(void* work, int B, int batch) {
+    const size_t used = 2 * (size_t)batch * B * (3 * B) * sizeof(float);
+    return (int*)((char*)work + ((used + 255) & ~(size_t)255));
 }
 
 int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int precision, void* work,
               cudaStream_t st) {
     int nprod;
-    S2G_TRY(check_prec(precision, &nprod));
+    bool f16;
+    S2G_TRY(check_prec(precision, &nprod, &f16));
     S2G_TRY(build_split(t));
     Split* s = (Split*)t->split;
     const int B = t->bw, S = 2 * B;
@@ -947,42 +1666,42 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
     // 2. weighted DCT-II per (function, seminaive order)                      (seminaive.c:161-176)
     S2G_TRY(fft_kernels(1, B, X, Cb, batch, s, st, 1.f));
     // 3. tensor-core contraction (seminaive orders from C, naive orders from X)
-    Leg p{};
-    p.C = Cb;
-    p.X = X;
-    p.rc = rc;
-    p.ic = ic;
-    p.blob = s->fwd_blob;
-    p.blob_off = s->fwd_off;
-    p.err = s->err;
-    p.B = B;
-    p.N = batch;
-    p.nprod = nprod;
-    return launch_leg(true, p, st);
+    LegSpec q{};
+    q.t = t;
+    q.N = batch;
+    q.C = Cb;
+    q.X = X;
+    q.rc = rc;
+    q.ic = ic;
+    return split_leg(true, precision, &q, 1, work_counter(work, B, batch), 0, st);
 }
 
 int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int batch, int precision, void* work,
                   cudaStream_t st) {
     int nprod;
-    S2G_TRY(check_prec(precision, &nprod));
-    S2G_TRY(build_split(t));
-    Split* s = (Split*)t->split;
+    bool f16;
+    S2G_TRY(check_prec(precision, &nprod, &f16));
     const int B = t->bw, S = 2 * B;
     float* F = (float*)work;
     float* Fc = F + 2 * (size_t)batch * B * S;
+    LegSpec q{};
+    q.t = t;
+    q.N = batch;
+    q.rc_in = rc;
+    q.ic_in = ic;
+    q.Fc = Fc;
+    q.F = F;
+    S2G_TRY(split_leg(false, precision, &q, 1, work_counter(work, B, batch), 0, st));
+    return split_inv_tail(t, F, Fc, grid, batch, nullptr, st);
+}
+
+// Inverse stages after the contraction: REDFT01 (+ sin(theta) for odd m), naive-order
+// recombination, DFT over the orders into the grid (gmap: per-function grid offsets or null).
+int split_inv_tail(Tables* t, float* F, float* Fc, float* grid, int batch, const int64_t* gmap, cudaStream_t st) {
+    S2G_TRY(build_split(t));
+    Split* s = (Split*)t->split;
+    const int B = t->bw, S = 2 * B;
     const float scale = (float)(1.0 / sqrt(2.0 * kPi));
-    Leg p{};
-    p.rc_in = rc;
-    p.ic_in = ic;
-    p.Fc = Fc;
-    p.F = F;
-    p.blob = s->inv_blob;
-    p.blob_off = s->inv_off;
-    p.err = s->err;
-    p.B = B;
-    p.N = batch;
-    p.nprod = nprod;
-    S2G_TRY(launch_leg(false, p, st));
     // REDFT01 (+ sin(theta) for odd m), scaled by 1/sqrt(2 pi)              (seminaive.c:105-114)
     S2G_TRY(fft_kernels(2, B, Fc, F, batch, s, st, scale));
     {
@@ -992,7 +1711,24 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
         S2G_CUDA(cudaGetLastError());
     }
     // DFT with sign +1 over the orders, Hermitian rows                      (FST_semi_memo.c:334-350)
-    return fft_kernels(3, B, F, grid, batch, s, st, 1.f);
+    return fft_kernels(3, B, F, grid, batch, s, st, 1.f, gmap);
+}
+
+int split_prepare(Tables* t, int precision) {
+    int nprod;
+    bool f16;
+    S2G_TRY(check_prec(precision, &nprod, &f16));
+    return f16 ? build_split16(t) : build_split(t);
+}
+
+// Forward stages before the contraction: DFT along phi and the weighted DCT-II.
+int split_fwd_head(Tables* t, const float* grid, float* X, float* C, int batch, const int64_t* gmap,
+                   cudaStream_t st) {
+    S2G_TRY(build_split(t));
+    Split* s = (Split*)t->split;
+    const int B = t->bw, S = 2 * B;
+    S2G_TRY(fft_kernels(0, B, grid, X, batch, s, st, (float)(sqrt(2.0 * kPi) / S), gmap));
+    return fft_kernels(1, B, X, C, batch, s, st, 1.f);
 }
 
 int split_device_status(Tables* t, int clear) {
@@ -1072,6 +1808,12 @@ __global__ void __launch_bounds__(128, 1) k_tc_selftest(int N, int K, int nprod,
 }
 
 }  // namespace s2g
+
+extern "C" int s2g_set_contraction_kernel(int which) {
+    if (which != 0 && which != 1) return s2g::fail(S2G_ERR_ARG, "contraction kernel %d (0 or 1)", which);
+    s2g::g_leg_kernel = which;
+    return S2G_OK;
+}
 
 extern "C" int s2g_selftest_tc(int N, int K, int nprod, const float* dA, const float* dB, float* dD) {
     using namespace s2g;

@@ -273,7 +273,7 @@ int generate_cos_pml_device(int bw, int m_begin, int m_end, double* d_fwd, const
     const Len L = make_len(bw);
     GenCos p{bw, m_begin, d_fwd, d_off, tw.twB, tw.twQ, tw.tw4, L.logn};
     const size_t smem = (size_t)(7 * bw + 2 * bw) * sizeof(double);
-    if (smem > 48 * 1024)
+    if (smem > 0)  // the 48 KiB default covers static plus dynamic shared memory
         S2G_CUDA(cudaFuncSetAttribute((const void*)k_gen_cos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     {
         ProfScope ps_("gen_cos_pml", st);
@@ -299,7 +299,7 @@ int transpose_cos_pml_device(int bw, int m_begin, int m_end, const double* d_fwd
 int generate_pml_device(int bw, int m_begin, int m_end, double* d_fwd, const int64_t* d_off, cudaStream_t st) {
     if (m_end <= m_begin) return S2G_OK;
     const size_t smem = (size_t)3 * 2 * bw * sizeof(double);
-    if (smem > 48 * 1024)
+    if (smem > 0)  // the 48 KiB default covers static plus dynamic shared memory
         S2G_CUDA(cudaFuncSetAttribute((const void*)k_gen_pml, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     {
         ProfScope ps_("gen_pml", st);

@@ -77,3 +77,40 @@ def test_config5_fp64_bw1024_roundtrip_and_conv():
     e = (torch.hypot(c_rc - tr, c_ic - ti).amax(1) / scale).max().item()
     assert e <= 1e-10, e
     assert ci.abs().max().item() <= 1e-10 * cr.abs().max().item()
+
+
+@pytest.mark.parametrize("prec", [api.PREC_BF16X3])
+def test_config5_split_bw1024_with_fp64_residual_refinement(prec):
+    """16 real functions at bw 1024: the split path alone, then with one FP64-residual refinement
+    step (forward and inverse) to <= 1e-10 against the FP64 path."""
+    import torch
+    bw, nb = 1024, 16
+    rng = np.random.default_rng(15)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    grid = torch.empty(nb, 4 * bw * bw, dtype=torch.float64, device="cuda")
+    plan.inv_fst(d_rc, d_ic, grid, None, nb, api.REAL)
+    f_rc, f_ic = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    plan.fst(grid, None, f_rc, f_ic, nb, api.REAL)
+    mag = torch.hypot(f_rc, f_ic).amax(1)
+    # split path alone (FP32 samples)
+    s_rc = torch.empty(nb, bw * bw, dtype=torch.float32, device="cuda")
+    s_ic = torch.empty_like(s_rc)
+    plan.fst_real_f32(grid.float(), s_rc, s_ic, nb, prec)
+    plan.sync_status()
+    e_split = (torch.hypot(s_rc.double() - f_rc, s_ic.double() - f_ic).amax(1) / mag).max().item()
+    assert e_split <= 2e-6, e_split
+    # refined forward
+    r_rc, r_ic = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    plan.fst_refined(grid, r_rc, r_ic, nb, prec)
+    plan.sync_status()
+    e_fwd = (torch.hypot(r_rc - f_rc, r_ic - f_ic).amax(1) / mag).max().item()
+    # refined inverse
+    r_grid = torch.empty_like(grid)
+    plan.inv_fst_refined(d_rc, d_ic, r_grid, nb, prec)
+    plan.sync_status()
+    e_inv = ((r_grid - grid).abs().amax(1) / grid.abs().amax(1)).max().item()
+    print(f"bw 1024: split {e_split:.2e}, refined forward {e_fwd:.2e}, refined inverse {e_inv:.2e}")
+    assert e_fwd <= 1e-10, e_fwd
+    assert e_inv <= 1e-10, e_inv

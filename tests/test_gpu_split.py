@@ -4,6 +4,8 @@ Error metric: normwise relative error max|x - x_ref| / max|x_ref| per function (
 for the forward, samples for the inverse), reference = FP64.  Stated tolerances:
   S2G_PREC_BF16X3 (6 split products, FP32 FFT/DCT): <= 1e-6   (BASELINE headline tolerance)
   S2G_PREC_BF16X2 (3 split products):               <= 1e-4
+  S2G_PREC_FP16X2 (2-term FP16, 3 products):        <= 2e-6 for bw <= 256, <= 5e-6 at bw 512
+    (two FP16 terms hold 22 bits: about 2^-22 per product before cancellation in the sums)
 """
 import numpy as np
 import pytest
@@ -12,7 +14,7 @@ from s2kit_gb300 import api
 from tests._util import real_field_coeffs
 
 pytestmark = pytest.mark.gpu
-TOL = {api.PREC_BF16X3: 1e-6, api.PREC_BF16X2: 1e-4}
+TOL = {api.PREC_BF16X3: 1e-6, api.PREC_BF16X2: 1e-4, api.PREC_FP16X2: 2e-6}
 
 
 def _torch():
@@ -60,7 +62,7 @@ def _nerr(got, ref):
 
 
 @pytest.mark.parametrize("bw,nb", [(16, 3), (32, 70), (64, 10), (128, 65), (256, 130), (512, 2)])
-@pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_BF16X2])
+@pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_BF16X2, api.PREC_FP16X2])
 def test_split_forward_inverse_vs_fp64(bw, nb, prec):
     torch = _torch()
     rng = np.random.default_rng(bw + nb)
@@ -82,8 +84,9 @@ def test_split_forward_inverse_vs_fp64(bw, nb, prec):
     ref_mag = torch.hypot(frc64, fic64).amax(dim=1)
     e_fwd = (torch.hypot(s_rc.double() - frc64, s_ic.double() - fic64).amax(dim=1) / ref_mag).max().item()
     e_inv = _nerr(s_grid, grid64)
-    assert e_fwd <= TOL[prec], e_fwd
-    assert e_inv <= TOL[prec], e_inv
+    tol = 5e-6 if (prec == api.PREC_FP16X2 and bw > 256) else TOL[prec]
+    assert e_fwd <= tol, e_fwd
+    assert e_inv <= tol, e_inv
 
 
 def test_split_matches_oracle_and_roundtrip(oracle):
@@ -140,3 +143,32 @@ def test_split_rejects_unsupported():
     plan64 = api.Plan(64, 64)
     with pytest.raises(s2.S2GError):
         plan64.fst_real_f32(x, x, x, 1, 7)  # unknown precision
+
+
+@pytest.mark.parametrize("bw,nb", [(16, 70), (64, 130), (256, 64), (512, 3)])
+@pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_FP16X2])
+def test_contraction_kernels_agree_bitwise(bw, nb, prec):
+    """The warp-specialised and the per-chunk-staged contraction kernels do the same arithmetic
+    per work item: forward and inverse outputs are identical bit for bit."""
+    torch = _torch()
+    lib = api.load()
+    rng = np.random.default_rng(bw * 7 + nb)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    c32r, c32i = torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda()
+    outs = []
+    try:
+        for which in (0, 1):
+            assert lib.s2g_set_contraction_kernel(which) == 0
+            g = torch.full((nb, 4 * bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+            plan.inv_fst_real_f32(c32r, c32i, g, nb, prec)
+            o_r = torch.full((nb, bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+            o_i = torch.full_like(o_r, float("nan"))
+            plan.fst_real_f32(g, o_r, o_i, nb, prec)
+            plan.sync_status()
+            outs.append((g, o_r, o_i))
+    finally:
+        lib.s2g_set_contraction_kernel(1)
+    for a, b in zip(*outs):
+        assert torch.isfinite(a).all()
+        assert torch.equal(a, b)
