@@ -46,6 +46,8 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--group", type=int, default=1, help="also time the grouped uneven-bandwidth workload")
+    ap.add_argument("--phase", default="all", choices=["all", "split"],
+                    help="split: only the warm-up and timed device-resident split steps (for profilers)")
     return ap.parse_args()
 
 
@@ -285,6 +287,15 @@ def main():
     ms = reduce_max(e0.elapsed_time(e1) / args.steps, dist, "cuda")
     value = weak_scaling_value(N, ws, ms)
     plan.sync_status()
+    if args.phase == "split":
+        clocks.stop()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": ms, "phase": "split", "config": config(args),
+                              "gpu_launches": int(launches)}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
 
     # ---- per-kernel event timing pass (same steps, every launch bracketed by events)
     import ctypes

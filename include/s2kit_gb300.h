@@ -183,8 +183,13 @@ int s2g_inv_fst_real_f32(s2g_plan plan, const float* rcoeffs, const float* icoef
 /* Real-field transforms with FP64 samples and coefficients whose Legendre contraction runs as
  * split products (precision: S2G_PREC_BF16X3, _BF16X2 or _FP16X2) followed by one refinement
  * step with an FP64 residual: forward a1 = F(f), a = a1 + F(f - I64(a1)); inverse g1 = I(a),
- * g = g1 + I(a - F64(g1)), where I64/F64 are the FP64 transforms on the GPU.  The error falls
- * from about e (the split path's) to about e^2 (below 1e-10 with BF16X3).  Layouts as
+ * g = g1 + I(a - F64(g1)), where I64/F64 are the FP64 transforms on the GPU.  Forward: the
+ * coefficient error falls from about e (the split path's) to about e^2 (below 1e-10 with
+ * BF16X3).  Inverse: the band-limited part of the sample error -- what a forward transform of
+ * the output sees, F64(g) - a -- falls to about e^2 as well, but the split synthesis rounds its
+ * samples to FP32, and that rounding noise lies outside the band the residual can see, so the
+ * pointwise sample error stays at the FP32 level (about 1e-7).  Both cost one FP64 transform
+ * (the residual) plus two split transforms.  Layouts as
  * s2g_fst_real_f32 (the inverse reads the non-negative orders); power-of-two bw in [16, 1024],
  * plan cutoff == bw.  The plan grows its own scratch. */
 int s2g_fst_refined(s2g_plan plan, const double* grid, double* rcoeffs, double* icoeffs, int batch, int precision,

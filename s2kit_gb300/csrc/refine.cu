@@ -8,6 +8,11 @@
 // takes the 3-term split BF16 path (e ~ 1e-6) below 1e-10.  The residual and the sums are FP64;
 // the two split transforms read FP32 samples/coefficients (the residual is small, so FP32 keeps
 // its relative precision).
+// The forward result is exact to e^2 only if the split forward leaves nothing the FP64 inverse
+// ignores: for a real field that is Im f(l,0), which the split DCT writes as exact zeros.
+// The inverse's samples g1 carry FP32 rounding noise that is not band-limited; F64 sees only
+// its band-limited part, so the refined samples are exact to e^2 in that part (F64(g) = a to
+// about e^2) while their pointwise error keeps the FP32 rounding of the split synthesis.
 #include "s2g_internal.h"
 
 namespace s2g {

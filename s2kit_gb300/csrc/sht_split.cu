@@ -512,13 +512,17 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(const float* __res
     const float nrm0 = 0.70710678118654752440f * nrm;
     float* cr = Cout + (size_t)row * B;
     float* ci = cr + (size_t)nrows * B;
+    // Order 0 of a real field has a real spectrum: its imaginary plane is zero on input, but the
+    // packed FFT's Hermitian halves do not cancel exactly in FP32, so store exact zeros (the
+    // reference's REDFT10 of the zero imaginary row gives exact zeros, FST_semi_memo.c:96-120).
+    const bool im_zero = (m == 0);
     for (int k = lane; k < B; k += 32) {
         const int kk = (S - k) & (S - 1);
         const float ar = wr[pad32(k)], ai = wi[pad32(k)], br = wr[pad32(kk)], bi = wi[pad32(kk)];
         const float c = twD[k].x, sn = twD[k].y;
         const float fct = (k == 0) ? nrm0 : nrm;
         cr[k] = ((ar + br) * c + (ai - bi) * sn) * fct;
-        ci[k] = ((ai + bi) * c - (ar - br) * sn) * fct;
+        ci[k] = im_zero ? 0.f : ((ai + bi) * c - (ar - br) * sn) * fct;
     }
 }
 

@@ -172,3 +172,24 @@ def test_contraction_kernels_agree_bitwise(bw, nb, prec):
     for a, b in zip(*outs):
         assert torch.isfinite(a).all()
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_FP16X2])
+@pytest.mark.parametrize("bw", [32, 256])
+def test_split_forward_zonal_imaginary_is_exact_zero(bw, prec):
+    """For real samples the reference's order-0 imaginary coefficients are exact zeros (the
+    REDFT10 of a zero row, FST_semi_memo.c:96-120); the split path must give the same zeros,
+    not FP32 rounding residue (which an FP64 REAL inverse ignores, so no refinement fixes it)."""
+    torch = _torch()
+    from tests._util import harmonic_index
+    rng = np.random.default_rng(bw + 7)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=4)
+    plan = api.Plan(bw, bw)
+    grid, _, _ = _fp64_pair(plan, rc, ic)
+    s_rc = torch.empty(4, bw * bw, dtype=torch.float32, device="cuda")
+    s_ic = torch.empty_like(s_rc)
+    plan.fst_real_f32(grid.float(), s_rc, s_ic, 4, prec)
+    plan.sync_status()
+    i0 = harmonic_index(0, np.arange(bw), bw)
+    assert (s_ic.cpu().numpy()[:, i0] == 0.0).all()
+    assert (s_rc.cpu().numpy()[:, i0] != 0.0).any()
