@@ -265,8 +265,10 @@ int s2g_selftest_tc(int N, int K, int nprod, const float* A, const float* B, flo
 
 /* Selects the tensor-core contraction kernel for later calls (process-wide): 1 (default) =
  * warp-specialised persistent kernel (scheduler/table-copy warp, MMA warp, A-producer warps,
- * epilogue warps; one CTA per SM), 0 = the kernel in which all threads stage each chunk (two
- * CTAs per SM).  Both do the same arithmetic per work item and give identical results. */
+ * epilogue warps; one CTA per SM) that moves its A operand -- and the inverse its output -- by
+ * tensor-map TMA where it can (one bandwidth class, BF16 terms, bw >= 64); 2 = the same kernel
+ * with per-thread asynchronous copies only; 0 = the kernel in which all threads stage each
+ * chunk (two CTAs per SM).  All do the same arithmetic per work item and give identical results. */
 int s2g_set_contraction_kernel(int which);
 
 /* Kernel timing: while enabled, every kernel the library launches is bracketed by CUDA

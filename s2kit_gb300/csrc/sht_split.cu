@@ -4,7 +4,7 @@
 // Forward (FSTSemiMemo, REAL, cutoff = bw; FST_semi_memo.c:68-145):
 //   k_rows_fwd_w       : DFT along phi (warp FFT, two real latitudes per warp), X[p][f][m][theta]
 //   k_dct_fwd_w        : weights (even/odd order) + REDFT10 + normalisation (seminaive.c:161-176)
-//                        -> C[p][f][m][k], k < bw
+//                        -> C[p][f][m][t][j], cosine frequency k = 2j + t (parity-split)
 //   k_leg_fwd_tc       : per (order m, 64 functions): for each parity t of (l - m), the dense
 //                        trapezoid T_{m,t}[i][j] = T(m, l = m+t+2i, k = 2j+t) times C (seminaive.c:183-197)
 //                        as D[128 x N] = A[128 x K] * B[N x K]^T on tcgen05, A = 64 functions x
@@ -26,6 +26,9 @@
 #include <atomic>
 #include <mutex>
 #include <vector>
+
+#include <cuda.h>  // CUtensorMap and its encoder's types (the encoder is fetched at run time)
+#include <cudaTypedefs.h>
 
 #include "s2g_common.cuh"
 #include "s2g_internal.h"
@@ -52,8 +55,9 @@ struct Split {
     int64_t* fwd16_off = nullptr;
     int64_t* inv16_off = nullptr;
     double tab16 = 0.0;
-    // per (direction, tile N): prefix sums over m of the contraction's work items per order
-    std::vector<std::pair<int, int*>> mstart[2];
+    // per (direction, tile N extent NB): the work items of one 64-function tile, in order, as
+    // (order m, index j within the order) -- item decoding is one load
+    std::vector<std::pair<int, int2*>> itab[2];
     int* err = nullptr;          // device error word (S2G_ERR_TIMEOUT on an expired wait)
     size_t fwd_bytes = 0, inv_bytes = 0;
 };
@@ -75,7 +79,7 @@ void free_split(Tables* t) {
     cudaFree(s->inv16);
     cudaFree(s->fwd16_off);
     cudaFree(s->inv16_off);
-    for (auto& v : s->mstart)
+    for (auto& v : s->itab)
         for (auto& e : v) cudaFree(e.second);
     cudaFree(s->err);
     delete s;
@@ -466,9 +470,12 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
     }
 }
 
-// Weighted REDFT10 per (function, seminaive order) row: C[p][f][m][k], k < B.
+// Weighted REDFT10 per (function, seminaive order) row, stored by parity of the cosine index:
+// C[p][f][m][t][j] holds frequency k = 2j + t (j < B/2), so that the contraction's operand rows
+// of one parity are contiguous.  Naive orders are folded in place in X for their contraction:
+// X[p][f][m][t][j] = x[j] + (-1)^t x[S-1-j], j < B (the even/odd latitude halves).
 template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(const float* __restrict__ X, float* __restrict__ Cout, int nrows,
+__global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict__ X, float* __restrict__ Cout, int nrows,
                                                    const float* __restrict__ gw, const float2* __restrict__ gtw,
                                                    const float2* __restrict__ gtwD) {
     constexpr int S = 32 * R, B = S / 2;
@@ -487,7 +494,25 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(const float* __res
     const int row = blockIdx.x * FftShape<R>::W + warp;
     if (row >= nrows) return;
     const int m = row % B;
-    if (naive_order(m)) return;
+    if (naive_order(m)) {
+        float* xr = X + (size_t)row * S;
+        float* xi = xr + (size_t)nrows * S;
+        float* wr = spr + warp * PS;
+        float* wi = spi + warp * PS;
+        for (int q = lane; q < S; q += 32) {
+            wr[q] = xr[q];
+            wi[q] = xi[q];
+        }
+        __syncwarp();
+        for (int j = lane; j < B; j += 32) {
+            const float ar = wr[j], br = wr[S - 1 - j], ai = wi[j], bi = wi[S - 1 - j];
+            xr[j] = ar + br;
+            xr[B + j] = ar - br;
+            xi[j] = ai + bi;
+            xi[B + j] = ai - bi;
+        }
+        return;
+    }
     const float* ws = w + ((m & 1) ? S : 0);
     const float* xr = X + (size_t)row * S;
     const float* xi = xr + (size_t)nrows * S;
@@ -521,8 +546,9 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(const float* __res
         const float ar = wr[pad32(k)], ai = wi[pad32(k)], br = wr[pad32(kk)], bi = wi[pad32(kk)];
         const float c = twD[k].x, sn = twD[k].y;
         const float fct = (k == 0) ? nrm0 : nrm;
-        cr[k] = ((ar + br) * c + (ai - bi) * sn) * fct;
-        ci[k] = im_zero ? 0.f : ((ai + bi) * c - (ar - br) * sn) * fct;
+        const int o = (k & 1) * (B / 2) + (k >> 1);
+        cr[o] = ((ar + br) * c + (ai - bi) * sn) * fct;
+        ci[o] = im_zero ? 0.f : ((ai + bi) * c - (ar - br) * sn) * fct;
     }
 }
 
@@ -548,6 +574,7 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     if (row >= nrows) return;
     const int m = row % B;
     if (naive_order(m)) return;
+    // Fc[p][f][m][t][j]: cosine coefficient k = 2j + t at (k & 1) * B/2 + k/2
     const float* xa = Fc + (size_t)row * B;
     const float* xb = xa + (size_t)nrows * B;
     float2 v[R];
@@ -555,8 +582,9 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     for (int i = 0; i < R; ++i) {
         const int k = lane + 32 * i;
         const int r = S - k;
-        const float ak = (k < B) ? xa[k] : 0.f, bk = (k < B) ? xb[k] : 0.f;
-        const float ar = (k > 0 && r < B) ? xa[r] : 0.f, br = (k > 0 && r < B) ? xb[r] : 0.f;
+        const int ok = (k & 1) * (B / 2) + (k >> 1), orr = (r & 1) * (B / 2) + (r >> 1);
+        const float ak = (k < B) ? xa[ok] : 0.f, bk = (k < B) ? xb[ok] : 0.f;
+        const float ar = (k > 0 && r < B) ? xa[orr] : 0.f, br = (k > 0 && r < B) ? xb[orr] : 0.f;
         const float wr = ak + br, wi = bk - ar;
         const float2 d = twD[k];
         v[i] = make_float2(wr * d.x - wi * d.y, wr * d.y + wi * d.x);
@@ -684,21 +712,31 @@ struct LegClass {
     int B, N, ntiles;         // bandwidth, functions, 64-function tiles
     int NB;                   // table rows per work item (N extent of the tile)
     int per_tile;             // work items per 64-function tile
-    const int* mstart;        // B + 1 prefix sums of the items of each order (within a tile)
+    const int2* itab;         // per_tile entries: (order m, index of the item within the order)
     int64_t item0;            // first work item of the class
     float tab_inv;            // inverse of the table blob's scale
-    const float* C;           // forward seminaive input C[p][f][m][k]
-    const float* X;           // forward naive input X[p][f][m][theta]
+    const float* C;           // forward seminaive input C[p][f][m][t][j] (k = 2j + t)
+    const float* X;           // forward naive input, folded halves X[p][f][m][t][j], j < B
     const float* rc_in;       // inverse input coefficients
     const float* ic_in;
     float* rc;                // forward output coefficients
     float* ic;
-    float* Fc;                // inverse seminaive output Fcos[p][f][m][k]
+    float* Fc;                // inverse seminaive output Fcos[p][f][m][t][j] (k = 2j + t)
     float* F;                 // inverse naive output (D0 | D1) in F[p][f][m][.]
     const int64_t* cmap;      // function -> element offset of its coefficients (null: f * B * B)
     const uint8_t* blob;
     const int64_t* blob_off;
 };
+
+// Tensor-map TMA path (one bandwidth class, BF16 terms, no coefficient map, bw >= 64): the A
+// operand of every chunk is one or two tiled TMA loads into a staging ring, and the inverse's
+// seminaive output leaves through tiled TMA stores.  Boxes (innermost first):
+//   forward seminaive: C      [p][f][m][t*B/2 + j]  box {32, 1, 64, 2}, 128-byte swizzle
+//   forward naive    : X      [p][f][m][t*B + j]    box {32, 1, 64, 2}, 128-byte swizzle
+//   inverse          : rc, ic [f][bw*bw]            box {kInvBox, 64} from the 16-byte aligned
+//                      element below the chunk's first coefficient (no swizzle)
+//   inverse output   : Fc     [p][f][m][t*B/2 + j]  box {32, 1, 64, 2}, 128-byte swizzle
+static constexpr int kInvBox = 68;     // 64 coefficients (both parities of 32 degrees) + 4 of alignment slack
 
 struct Leg {
     LegClass cls[kMaxClasses];
@@ -707,6 +745,10 @@ struct Leg {
     long long nitems;
     int* counter;             // work counter, zero at launch
     int* err;
+    int tma;                  // 1: tensor-map TMA path (below)
+    uint32_t a_chunk_bytes;   // TMA bytes of one A chunk
+    CUtensorMap tmA0, tmA1;   // forward: C, folded X; inverse: rc, ic
+    CUtensorMap tmO;          // inverse: Fc
 };
 
 __constant__ int c_prod_a[6] = {0, 0, 1, 0, 1, 2};
@@ -727,56 +769,41 @@ __device__ __forceinline__ int64_t coef_base(const LegClass& k, int f) {
 }
 
 // 8 consecutive K entries of parity t for row r, segment seg of chunk c, as FP32.
+//   forward seminaive: C[p][f][m][t][j], j < B/2 (parity-split DCT output)
+//   forward naive    : X[p][f][m][t][j], j < B (latitude halves folded by the DCT kernel)
+//   inverse          : a(l), l - m = 2i + t, from the coefficient arrays (stride 2)
+template <bool FWD>
+__device__ __forceinline__ const float* fwd_row(const LegClass& k, int m, bool nv, int t, int f, int part) {
+    const int B = k.B;
+    return nv ? k.X + (((size_t)part * k.N + f) * B + m) * (2 * B) + t * B
+              : k.C + (((size_t)part * k.N + f) * B + m) * B + t * (B / 2);
+}
+
 template <bool FWD>
 __device__ __forceinline__ void load_seg(const LegClass& k, int m, bool nv, int t, int f, int part, int c, int seg,
                                          float* v) {
-    const int B = k.B, S = 2 * B;
+    const int B = k.B;
     if (f >= k.N) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[q] = 0.f;
         return;
     }
-    if (FWD && nv) {
-        // folded latitudes: x[j] +/- x[S-1-j], j = c*KC + seg*8 + q < B
-        const int j0 = c * kKC + seg * 8;
-        if (j0 >= B) {
+    const int j0 = c * kKC + seg * 8;
+    if (FWD) {
+        if (j0 >= (nv ? B : B / 2)) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) v[q] = 0.f;
             return;
         }
-        const float* row = k.X + (((size_t)part * k.N + f) * B + m) * S;
-        const float4 a0 = reinterpret_cast<const float4*>(row + j0)[0];
-        const float4 a1 = reinterpret_cast<const float4*>(row + j0)[1];
-        const float4 b0 = reinterpret_cast<const float4*>(row + S - 8 - j0)[0];
-        const float4 b1 = reinterpret_cast<const float4*>(row + S - 8 - j0)[1];
-        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        const float b[8] = {b1.w, b1.z, b1.y, b1.x, b0.w, b0.z, b0.y, b0.x};  // x[S-1-j0-q]
-        const float sg = t ? -1.f : 1.f;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = a[q] + sg * b[q];
-        return;
-    }
-    // 16 consecutive source entries, parity t taken: forward C[k], k = 2j + t; inverse a(l), l-m = 2i + t
-    const int kb = 2 * (c * kKC + seg * 8);
-    if (FWD) {
-        const float* src = k.C + (((size_t)part * k.N + f) * B + m) * B + kb;
-        if (kb < B) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float4 x = reinterpret_cast<const float4*>(src)[q];
-                v[2 * q] = t ? x.y : x.x;
-                v[2 * q + 1] = t ? x.w : x.z;
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < 8; ++q) v[q] = 0.f;
-        }
+        const float4* src = reinterpret_cast<const float4*>(fwd_row<FWD>(k, m, nv, t, f, part) + j0);
+        const float4 a = src[0], b = src[1];
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
     } else {
         const float* src = (part ? k.ic_in : k.rc_in) + coef_base(k, f) + index_of_harmonic_coeff(m, m, B);
         const int lim = B - m;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const int d = kb + 2 * q + t;
+            const int d = 2 * (j0 + q) + t;
             v[q] = (d < lim) ? src[d] : 0.f;
         }
     }
@@ -885,11 +912,8 @@ __device__ __forceinline__ void epi_store(const LegClass& K, int m, int t, int n
             const int f = f0 + (r & 63), part = r >> 6;
             if (f >= K.N) continue;
             const float* src = ep + r * ES;
-            float* dst = K.Fc + (((size_t)part * K.N + f) * B + m) * B + t;
-            for (int j = lane; j < nj; j += 32) {
-                const int kk = 2 * (c0 + j);
-                dst[kk] = src[j] * ((kk + t) == 0 ? sc0 : sc_);
-            }
+            float* dst = K.Fc + (((size_t)part * K.N + f) * B + m) * B + t * (B / 2) + c0;
+            for (int j = lane; j < nj; j += 32) dst[j] = src[j] * ((c0 + j + t) == 0 ? sc0 : sc_);
         }
     } else {
         for (int r = wid; r < 128; r += nw) {
@@ -958,13 +982,8 @@ __global__ void __launch_bounds__(kTPB, 2) k_leg_tc(Leg p, uint32_t stage_bytes,
                 const LegClass& K = p.cls[ci];
                 const long long li = item - K.item0;
                 const int rem = (int)(li % K.per_tile);
-                int lo = 0, hi = K.B - 1;  // largest m with mstart[m] <= rem
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (K.mstart[mid] <= rem) lo = mid;
-                    else hi = mid - 1;
-                }
-                const int j = rem - K.mstart[lo];
+                const int2 mj = K.itab[rem];
+                const int lo = mj.x, j = mj.y;
                 const int nsub = (geo(FWD, K.B, lo).NP + K.NB - 1) / K.NB;
                 s_dec[0] = ci;
                 s_dec[1] = lo;
@@ -1122,9 +1141,11 @@ static constexpr int kWsThreads = 512;
 static constexpr int kNI = 4;          // item ring entries
 static constexpr int kNAS = 2;         // A stages
 static constexpr int kMaxNBS = 8;      // table stages (upper bound)
-static constexpr int kEpiCols = 128;   // epilogue staging width
+static constexpr int kEpiCols = 64;    // epilogue staging width
+static constexpr int kMaxStg = 4;      // cp.async staging stages of the BF16 A producers (upper bound)
 static constexpr int kAProd = 256;     // A-producer threads
 static constexpr int kEpi = 128;       // epilogue threads
+static constexpr uint32_t kStgBytes = kAProd * kTasks * 8 * sizeof(float);  // one staging stage (16 KB)
 
 struct WsItem {
     int ci, m, t, sub, nb, f0;
@@ -1142,13 +1163,8 @@ __device__ __forceinline__ WsItem decode_item(const Leg& p, long long item) {
     const LegClass& K = p.cls[ci];
     const long long li = item - K.item0;
     const int rem = (int)(li % K.per_tile);
-    int lo = 0, hi = K.B - 1;  // largest m with mstart[m] <= rem
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (K.mstart[mid] <= rem) lo = mid;
-        else hi = mid - 1;
-    }
-    const int j = rem - K.mstart[lo];
+    const int2 mj = K.itab[rem];
+    const int lo = mj.x, j = mj.y;
     const int nsub = (geo(FWD, K.B, lo).NP + K.NB - 1) / K.NB;
     e.ci = ci;
     e.m = lo;
@@ -1159,9 +1175,242 @@ __device__ __forceinline__ WsItem decode_item(const Leg& p, long long item) {
     return e;
 }
 
+// BF16 A producers with asynchronous copies.  Each producer thread owns the same two
+// (row, 8-column segment) tasks of every chunk and stages their FP32 values through a private
+// ring of `nstg` stages in shared memory (cp.async, 16-byte pieces for the contiguous forward
+// rows, 4-byte pieces for the inverse's stride-2 coefficient gathers), so up to nstg chunks of
+// this CTA's A operand are in flight at once, across item boundaries.  A thread reads back only
+// what it copied itself, so its own cp.async groups order everything; no cross-thread barrier.
+__device__ __forceinline__ float4* stg_at(float4* stg, int s, int q, int h, int tid) {
+    return stg + ((s * kTasks + q) * 2 + h) * kAProd + tid;
+}
+
+template <bool FWD>
+__device__ __forceinline__ void issue_chunk(const LegClass& K, const WsItem& e, int c, float4* stg, int s, int tid) {
+    const int B = K.B;
+    const bool nv = FWD && naive_order(e.m);
+    constexpr int segs = kKC / 8;
+#pragma unroll
+    for (int q = 0; q < kTasks; ++q) {
+        const int task = tid + q * kAProd;
+        const int r = task / segs, seg = task - r * segs;
+        const int f = e.f0 + (r & 63), part = r >> 6;
+        const int j0 = c * kKC + seg * 8;
+        float4* d0 = stg_at(stg, s, q, 0, tid);
+        float4* d1 = stg_at(stg, s, q, 1, tid);
+        if (FWD) {
+            // rows are 32-byte aligned: C rows are B/2 floats apart, folded X rows B, and j0 % 8 == 0
+            const bool ok = f < K.N && j0 < (nv ? B : B / 2);
+            const float* src = ok ? fwd_row<FWD>(K, e.m, nv, e.t, f, part) + j0 : (nv ? K.X : K.C);
+            tc::cp_async16(d0, src, ok ? 16u : 0u);
+            tc::cp_async16(d1, ok ? src + 4 : src, ok ? 16u : 0u);
+        } else {
+            const bool fok = f < K.N;
+            const float* row =
+                fok ? (part ? K.ic_in : K.rc_in) + coef_base(K, f) + index_of_harmonic_coeff(e.m, e.m, B) : K.rc_in;
+            const int lim = B - e.m;
+            float* a = reinterpret_cast<float*>(d0);
+            float* b = reinterpret_cast<float*>(d1);
+#pragma unroll
+            for (int x = 0; x < 8; ++x) {
+                const int d = 2 * (j0 + x) + e.t;
+                const bool ok = fok && d < lim;
+                tc::cp_async4((x < 4 ? a : b) + (x & 3), ok ? row + d : K.rc_in, ok ? 4u : 0u);
+            }
+        }
+    }
+}
+
+template <bool FWD>
+__device__ __forceinline__ void produce_a_async(const Leg& p, uint8_t* smem, float4* stg, int nstg,
+                                                const WsItem* items, uint64_t* item_full, uint64_t* item_empty,
+                                                uint64_t* a_full, uint64_t* a_empty, volatile int* s_abort, int tid) {
+    constexpr uint32_t kAStage = 3 * kATile;
+    const unsigned full = 0xffffffffu;
+    uint32_t ac = 0;                 // A tiles produced (position in the A ring)
+    uint32_t n_iss = 0, n_con = 0;   // chunks issued into / consumed from the staging ring
+    int ki = 0, ci = 0, nch_i = 0;   // issue cursor: item, chunk, chunks of that item
+    WsItem ei{};
+    bool have_ei = false, iss_done = false;
+    float sc[kTasks];
+#pragma unroll
+    for (int q = 0; q < kTasks; ++q) sc[q] = 1.f;
+    // Fill free staging stages.  Waits (bounded) for an unpublished item only when nothing is in
+    // flight; every decision is warp-uniform.  Returns false when a wait expired.
+    auto top_up = [&]() -> bool {
+        while (!iss_done && n_iss - n_con < (uint32_t)nstg) {
+            if (!have_ei) {
+                const int sl = ki % kNI;
+                const uint32_t ph = (ki / kNI) & 1;
+                if (!__all_sync(full, tc::mbar_try_wait(&item_full[sl], ph))) {
+                    if (n_iss != n_con) return true;
+                    if (!__all_sync(full, tc::mbar_wait(&item_full[sl], ph))) return false;
+                }
+                ei = items[sl];
+                if (ei.ci < 0) {
+                    iss_done = true;
+                    break;
+                }
+                have_ei = true;
+                ci = 0;
+                nch_i = geo(FWD, p.cls[ei.ci].B, ei.m).nch;
+            }
+            issue_chunk<FWD>(p.cls[ei.ci], ei, ci, stg, (int)(n_iss % (uint32_t)nstg), tid);
+            tc::cp_async_commit();
+            ++n_iss;
+            if (++ci == nch_i) {
+                have_ei = false;
+                ++ki;
+            }
+        }
+        return true;
+    };
+    for (int k = 0; !*s_abort; ++k) {
+        const int slot = k % kNI;
+        if (!__all_sync(full, tc::mbar_wait(&item_full[slot], (k / kNI) & 1))) {
+            *s_abort = 1;
+            break;
+        }
+        const WsItem e = items[slot];
+        tc::mbar_arrive(&item_empty[slot]);
+        if (e.ci < 0) break;
+        const int nch = geo(FWD, p.cls[e.ci].B, e.m).nch;
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++ac) {
+            // chunk (k, c) is the oldest one issued: the issue cursor never falls behind
+            if (!top_up() || n_iss == n_con) {
+                ok = false;
+                break;
+            }
+            tc::cp_async_wait((int)(n_iss - n_con) - 1);
+            float va[kTasks][8];
+            const int ss = (int)(n_con % (uint32_t)nstg);
+#pragma unroll
+            for (int q = 0; q < kTasks; ++q) {
+                const float4 a = *stg_at(stg, ss, q, 0, tid), b = *stg_at(stg, ss, q, 1, tid);
+                va[q][0] = a.x, va[q][1] = a.y, va[q][2] = a.z, va[q][3] = a.w;
+                va[q][4] = b.x, va[q][5] = b.y, va[q][6] = b.z, va[q][7] = b.w;
+            }
+            ++n_con;
+            const int s = ac % kNAS;
+            if (!tc::mbar_wait(&a_empty[s], ((ac / kNAS) & 1) ^ 1)) {
+                ok = false;
+                break;
+            }
+            store_a<false>(smem + s * kAStage, va, sc, tid);
+            tc::fence_proxy_async_smem();
+            tc::mbar_arrive(&a_full[s]);
+        }
+        if (!ok) {
+            *s_abort = 1;
+            break;
+        }
+    }
+    tc::cp_async_wait(0);  // no copy lands in shared memory after this role has left
+}
+
+// BF16 A producers fed by tensor-map TMA: the scheduler warp loads each chunk's A operand
+// (FP32) into a staging ring; the producers split their two tasks' values into BF16 terms.
+template <bool FWD>
+__device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const uint8_t* stg, uint32_t stg_stride,
+                                              int nstg, const WsItem* items, uint64_t* item_full, uint64_t* item_empty,
+                                              uint64_t* stg_full, uint64_t* stg_empty, uint64_t* a_full,
+                                              uint64_t* a_empty, volatile int* s_abort, int tid) {
+    constexpr uint32_t kAStage = 3 * kATile;
+    constexpr int segs = kKC / 8;
+    const unsigned full = 0xffffffffu;
+    uint32_t ac = 0, sc = 0;  // A tiles produced, staging chunks consumed
+    float one[kTasks];
+#pragma unroll
+    for (int q = 0; q < kTasks; ++q) one[q] = 1.f;
+    for (int k = 0; !*s_abort; ++k) {
+        const int slot = k % kNI;
+        if (!__all_sync(full, tc::mbar_wait(&item_full[slot], (k / kNI) & 1))) {
+            *s_abort = 1;
+            break;
+        }
+        const WsItem e = items[slot];
+        tc::mbar_arrive(&item_empty[slot]);
+        if (e.ci < 0) break;
+        const LegClass& K = p.cls[e.ci];
+        const int B = K.B, m = e.m, t = e.t;
+        const bool nv = FWD && naive_order(m);
+        const int nch = geo(FWD, B, m).nch;
+        const int base = FWD ? 0 : index_of_harmonic_coeff(m, m, B);
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++ac, ++sc) {
+            const int ss = (int)(sc % (uint32_t)nstg);
+            if (!tc::mbar_wait(&stg_full[ss], (sc / nstg) & 1)) {
+                ok = false;
+                break;
+            }
+            const uint8_t* sb = stg + (size_t)ss * stg_stride;
+            float va[kTasks][8];
+#pragma unroll
+            for (int q = 0; q < kTasks; ++q) {
+                const int task = tid + q * kAProd;
+                const int r = task / segs, seg = task - r * segs;
+                const int j0 = c * kKC + seg * 8;
+                if (FWD) {
+                    // 128-byte rows (p, f), 16-byte chunk u of row r stored at chunk u ^ (r % 8)
+                    const bool valid = j0 < (nv ? B : B / 2);
+                    const float4 a = *reinterpret_cast<const float4*>(sb + r * 128 + (((2 * seg) ^ (r & 7)) << 4));
+                    const float4 b = *reinterpret_cast<const float4*>(sb + r * 128 + (((2 * seg + 1) ^ (r & 7)) << 4));
+                    va[q][0] = valid ? a.x : 0.f, va[q][1] = valid ? a.y : 0.f;
+                    va[q][2] = valid ? a.z : 0.f, va[q][3] = valid ? a.w : 0.f;
+                    va[q][4] = valid ? b.x : 0.f, va[q][5] = valid ? b.y : 0.f;
+                    va[q][6] = valid ? b.z : 0.f, va[q][7] = valid ? b.w : 0.f;
+                } else {
+                    // planes [p][64 functions][kInvBox]; the box starts at the 16-byte aligned element
+                    // at or below the chunk's first coefficient base + 64 c
+                    const int o = (base + c * 64) & 3;
+                    const float* row = reinterpret_cast<const float*>(sb) + (r >> 6) * (64 * kInvBox) +
+                                       (r & 63) * kInvBox + o;
+                    const int lim = B - m - c * 64;
+#pragma unroll
+                    for (int x = 0; x < 8; ++x) {
+                        const int d = 2 * (seg * 8 + x) + t;
+                        va[q][x] = d < lim ? row[d] : 0.f;
+                    }
+                }
+            }
+            tc::mbar_arrive(&stg_empty[ss]);
+            const int s = ac % kNAS;
+            if (!tc::mbar_wait(&a_empty[s], ((ac / kNAS) & 1) ^ 1)) {
+                ok = false;
+                break;
+            }
+            store_a<false>(smem + s * kAStage, va, one, tid);
+            tc::fence_proxy_async_smem();
+            tc::mbar_arrive(&a_full[s]);
+        }
+        if (!ok) {
+            *s_abort = 1;
+            break;
+        }
+    }
+}
+
+// TMA loads of the A operand of chunk c of item e into staging buffer dst (scheduler thread).
+template <bool FWD>
+__device__ __forceinline__ void issue_a_tma(const Leg& p, const WsItem& e, int c, uint8_t* dst, uint64_t* bar) {
+    const int B = p.cls[0].B;
+    tc::mbar_arrive_expect_tx(bar, p.a_chunk_bytes);
+    if (FWD) {
+        const bool nv = naive_order(e.m);
+        const int x = (nv ? e.t * B : e.t * (B / 2)) + c * kKC;
+        tc::tma_load_4d(dst, nv ? (const void*)&p.tmA1 : (const void*)&p.tmA0, x, e.m, e.f0, 0, bar);
+    } else {
+        const int x0 = (index_of_harmonic_coeff(e.m, e.m, B) + c * 64) & ~3;
+        tc::tma_load_2d(dst, &p.tmA0, x0, e.f0, bar);
+        tc::tma_load_2d(dst + 64 * kInvBox * sizeof(float), &p.tmA1, x0, e.f0, bar);
+    }
+}
+
 template <bool FWD, bool F16>
 __global__ void __launch_bounds__(kWsThreads, 1)
-    k_leg_ws(Leg p, uint32_t b_off, uint32_t b_stage, int nbs, uint32_t epi_off, uint32_t ncols, int nacc) {
+    k_leg_ws(const __grid_constant__ Leg p, uint32_t b_off, uint32_t b_stage, int nbs, uint32_t epi_off,
+             uint32_t ncols, int nacc, uint32_t stg_off, int nstg, uint32_t stg_stride) {
     constexpr int NT = F16 ? 2 : 3;
     constexpr uint32_t kAStage = NT * kATile;
     extern __shared__ __align__(1024) uint8_t dsm[];
@@ -1169,6 +1418,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     __shared__ uint64_t item_full[kNI], item_empty[kNI], sc_full[kNI];
     __shared__ uint64_t a_full[kNAS], a_empty[kNAS], b_full[kMaxNBS], b_empty[kMaxNBS];
     __shared__ uint64_t acc_full[2], acc_empty[2], fin;
+    __shared__ uint64_t stg_full[kMaxStg], stg_empty[kMaxStg];  // tensor-map path: A staging ring
     __shared__ WsItem items[kNI];
     __shared__ float s_rinv[kNI][128];
     __shared__ uint32_t tmem_slot;
@@ -1194,6 +1444,10 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             tc::mbar_init(&acc_empty[i], kEpi);
         }
         tc::mbar_init(&fin, 1);
+        for (int i = 0; i < kMaxStg; ++i) {
+            tc::mbar_init(&stg_full[i], 1);
+            tc::mbar_init(&stg_empty[i], kAProd);
+        }
         tc::fence_mbar_init();
         s_abort = 0;
     }
@@ -1208,7 +1462,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     if (warp == 0) {
         // ---------------- scheduler + table producer ----------------
         if (lane == 0) {
-            uint32_t bc = 0;  // table chunks issued
+            uint32_t bc = 0;   // table chunks issued
+            uint32_t stc = 0;  // A chunks loaded by TMA (tensor-map path)
             for (int k = 0; !s_abort; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_empty[slot], ((k / kNI) & 1) ^ 1)) {
@@ -1231,11 +1486,22 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                         break;
                     }
                     issue_table<F16>(smem + b_off + s * b_stage, blob, g.NP, n0, rows, c, &b_full[s]);
+                    if (!F16 && p.tma) {
+                        const int ss = (int)(stc % (uint32_t)nstg);
+                        if (!tc::mbar_wait(&stg_empty[ss], ((stc / nstg) & 1) ^ 1)) {
+                            s_abort = 1;
+                            break;
+                        }
+                        issue_a_tma<FWD>(p, e, c, smem + stg_off + (size_t)ss * stg_stride, &stg_full[ss]);
+                        ++stc;
+                    }
                 }
             }
             // copies in flight land before the CTA leaves (immediate on the normal path)
             for (uint32_t j = bc > (uint32_t)nbs ? bc - nbs : 0; j < bc; ++j)
                 tc::mbar_wait(&b_full[j % nbs], (j / nbs) & 1);
+            for (uint32_t j = stc > (uint32_t)nstg ? stc - nstg : 0; j < stc; ++j)
+                tc::mbar_wait(&stg_full[j % nstg], (j / nstg) & 1);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
@@ -1298,6 +1564,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
         const int et = threadIdx.x - 128;  // accumulator row = TMEM lane
         float* ep = reinterpret_cast<float*>(smem + epi_off);
         constexpr int ES = kEpiCols + 1;   // odd row stride
+        uint32_t eblk = 0;                 // TMA-store blocks written (staging buffer eblk & 1)
         for (int k = 0;; ++k) {
             const int slot = k % kNI;
             const int buf = k % nacc;
@@ -1323,6 +1590,42 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             const float rs = F16 ? s_rinv[slot][et] * K.tab_inv : 1.f;
             tc::tc_fence_after();
             const uint32_t trow = tmem + buf * accw + ((uint32_t)((warp & 3) * 32) << 16);
+            if (!FWD && p.tma && !naive_order(m)) {
+                // 32-column blocks: TMEM -> 128-byte swizzled staging (two buffers) -> one TMA store
+                const float sc_ = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
+                for (int cb0 = 0; cb0 < rows; cb0 += 32, ++eblk) {
+                    uint8_t* eb = reinterpret_cast<uint8_t*>(ep) + (eblk & 1) * 16384;
+                    if (et == 0) tc::bulk_wait_read1();  // the store that last read this buffer is done
+                    tc::named_bar_sync(1, kEpi);
+                    float v[32];
+                    ld_sum(trow + cb0, corr, p.nprod > 1, v);
+                    ld_sum(trow + cb0 + 16, corr, p.nprod > 1, v + 16);
+                    if (cb0 + 32 >= rows) {  // last TMEM read of this item: release the buffer
+                        tc::tc_fence_before();
+                        tc::mbar_arrive(&acc_empty[buf]);
+                    }
+                    const int j0 = n0 + cb0;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        float4 w4 = make_float4(v[4 * u] * sc_, v[4 * u + 1] * sc_, v[4 * u + 2] * sc_,
+                                                v[4 * u + 3] * sc_);
+                        if (u == 0 && j0 == 0 && t == 0) w4.x = v[0] * sc0;
+                        *reinterpret_cast<float4*>(eb + et * 128 + ((u ^ (et & 7)) << 4)) = w4;
+                    }
+                    tc::fence_proxy_async_smem();
+                    tc::named_bar_sync(1, kEpi);
+                    if (et == 0) {
+                        tc::tma_store_4d(&p.tmO, t * (B / 2) + j0, m, e.f0, 0, eb);
+                        tc::bulk_commit();
+                    }
+                }
+                tc::mbar_arrive(&item_empty[slot]);
+                continue;
+            }
+            if (!FWD && p.tma) {  // the plain path below reuses the staging: no store may still read it
+                if (et == 0) tc::bulk_wait_read0();
+                tc::named_bar_sync(1, kEpi);
+            }
             for (int cb0 = 0; cb0 < rows; cb0 += kEpiCols) {
                 const int w = min(kEpiCols, rows - cb0);
                 for (int cb = 0; cb < w; cb += 16) {
@@ -1341,8 +1644,17 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             }
             tc::mbar_arrive(&item_empty[slot]);
         }
+        if (et == 0) tc::bulk_wait_all();  // TMA stores complete before the CTA leaves
+    } else if (warp >= 8 && !F16 && p.tma) {
+        // ---------------- A producers (BF16 terms): staging filled by tensor-map TMA ----------------
+        produce_a_tma<FWD>(p, smem, smem + stg_off, stg_stride, nstg, items, item_full, item_empty, stg_full,
+                           stg_empty, a_full, a_empty, &s_abort, threadIdx.x - 256);
+    } else if (warp >= 8 && !F16) {
+        // ---------------- A producers (BF16 terms): asynchronous staging ----------------
+        produce_a_async<FWD>(p, smem, reinterpret_cast<float4*>(smem + stg_off), nstg, items, item_full, item_empty,
+                             a_full, a_empty, &s_abort, threadIdx.x - 256);
     } else if (warp >= 8) {
-        // ---------------- A producers ----------------
+        // ---------------- A producers (FP16 terms): row scales first, loads in registers ----------------
         const int tid = threadIdx.x - 256;
         uint32_t ac = 0;
         float va[kTasks][8];
@@ -1465,7 +1777,9 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     const uint32_t ncols = pair * nacc;
     const size_t a_bytes = (size_t)kNAS * nt * kATile;
     const size_t b_stage = (size_t)nt * nbmax * kKC * 2;
-    const size_t epi = (size_t)128 * (kEpiCols + 1) * sizeof(float);
+    // epilogue staging: the padded tile of the plain stores (and, on the tensor-map path of the
+    // inverse, two 16 KB swizzled TMA-store buffers in the same place), 1024-byte multiple
+    const size_t epi = ((size_t)128 * (kEpiCols + 1) * sizeof(float) + 1023) & ~(size_t)1023;
     int dev = 0, optin = 0, nsm = 0;
     S2G_CUDA(cudaGetDevice(&dev));
     S2G_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1473,51 +1787,122 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     cudaFuncAttributes fa{};
     S2G_CUDA(cudaFuncGetAttributes(&fa, fn));
     const long long budget = (long long)optin - (long long)fa.sharedSizeBytes - 1024;
-    const long long nbs_fit = (budget - (long long)a_bytes - (long long)epi) / (long long)b_stage;
+    // A staging: tensor-map path, one TMA box per stage (1024-byte multiple: swizzled boxes);
+    // cp.async path, per-thread slots.  As many stages as leave room for two table stages.
+    const size_t stg_stride = p.tma ? ((size_t)p.a_chunk_bytes + 1023) & ~(size_t)1023 : kStgBytes;
+    int nstg = f16 ? 0 : kMaxStg;
+    const int nstg_min = p.tma ? 1 : 2;
+    long long nbs_fit = 0;
+    for (;;) {
+        nbs_fit = (budget - (long long)a_bytes - (long long)nstg * (long long)stg_stride - (long long)epi) /
+                  (long long)b_stage;
+        if (nbs_fit >= 2 || nstg <= nstg_min || f16) break;
+        --nstg;
+    }
     const int nbs = (int)std::min<long long>(kMaxNBS, nbs_fit);
     if (nbs < 2) return fail(S2G_ERR_UNSUPPORTED, "warp-specialised contraction does not fit in shared memory");
-    const size_t smem = 1024 + a_bytes + (size_t)nbs * b_stage + epi;
+    const size_t stg_bytes = (size_t)nstg * stg_stride;
+    const size_t smem = 1024 + a_bytes + stg_bytes + (size_t)nbs * b_stage + epi;
     S2G_TRY(set_smem(fn, smem));
     const int grid = (int)std::min<long long>(items, nsm);
     S2G_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
-    const uint32_t b_off = (uint32_t)a_bytes, epi_off = (uint32_t)(a_bytes + nbs * b_stage);
+    const uint32_t stg_off = (uint32_t)a_bytes, b_off = (uint32_t)(a_bytes + stg_bytes),
+                   epi_off = (uint32_t)(a_bytes + stg_bytes + nbs * b_stage);
+    const uint32_t bs = (uint32_t)b_stage, ss = (uint32_t)stg_stride;
     {
         ProfScope ps_(fwd ? "leg_tc_fwd" : "leg_tc_inv", st);
         if (fwd && f16)
-            k_leg_ws<true, true><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols, nacc);
+            k_leg_ws<true, true><<<grid, kWsThreads, smem, st>>>(p, b_off, bs, nbs, epi_off, ncols, nacc, stg_off, nstg, ss);
         else if (fwd)
-            k_leg_ws<true, false><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols, nacc);
+            k_leg_ws<true, false><<<grid, kWsThreads, smem, st>>>(p, b_off, bs, nbs, epi_off, ncols, nacc, stg_off, nstg, ss);
         else if (f16)
-            k_leg_ws<false, true><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols, nacc);
+            k_leg_ws<false, true><<<grid, kWsThreads, smem, st>>>(p, b_off, bs, nbs, epi_off, ncols, nacc, stg_off, nstg, ss);
         else
-            k_leg_ws<false, false><<<grid, kWsThreads, smem, st>>>(p, b_off, (uint32_t)b_stage, nbs, epi_off, ncols,
-                                                                   nacc);
+            k_leg_ws<false, false><<<grid, kWsThreads, smem, st>>>(p, b_off, bs, nbs, epi_off, ncols, nacc, stg_off, nstg,
+                                                                   ss);
     }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
 
-// Device table of the work items of each order for tile N extent NB: order m has
-// 2 (parities) x nblk(m) (latitude blocks) x ceil(NP(m) / NB) (sub-blocks) items.
-static int get_mstart(Split* s, bool fwd, int NB, const int** out, int* per_tile) {
+// cuTensorMapEncodeTiled from the driver (fetched once through the runtime; no libcuda link).
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+    });
+    return fn;
+}
+
+// FP32 tiled map: dims/strides innermost first (strides in bytes for dims 1..rank-1).
+static bool encode_map(CUtensorMap* m, const void* base, int rank, const uint64_t* dims, const uint64_t* strides,
+                       const uint32_t* box, bool swz) {
+    auto fn = tmap_encoder();
+    if (!fn || ((uintptr_t)base & 15)) return false;
+    const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, const_cast<void*>(base), (const cuuint64_t*)dims,
+              (const cuuint64_t*)strides, (const cuuint32_t*)box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              swz ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Sets up the tensor-map path for a one-class launch; false leaves the launch on the other path.
+static bool setup_tma(Leg& p, bool fwd, const LegSpec& q) {
+    const int B = q.t->bw;
+    const uint64_t N = (uint64_t)q.N, b = (uint64_t)B;
+    const uint32_t box4[4] = {32, 1, 64, 2};
+    if (fwd) {
+        const uint64_t dc[4] = {b, b, N, 2}, sc[3] = {b * 4, b * b * 4, N * b * b * 4};
+        const uint64_t dx[4] = {2 * b, b, N, 2}, sx[3] = {2 * b * 4, 2 * b * b * 4, 2 * N * b * b * 4};
+        if (!encode_map(&p.tmA0, q.C, 4, dc, sc, box4, true) || !encode_map(&p.tmA1, q.X, 4, dx, sx, box4, true))
+            return false;
+        p.a_chunk_bytes = 32 * 64 * 2 * sizeof(float);
+    } else {
+        const uint64_t dcoef[2] = {b * b, N}, scoef[1] = {b * b * 4};
+        const uint32_t boxc[2] = {(uint32_t)kInvBox, 64};
+        const uint64_t dc[4] = {b, b, N, 2}, sc[3] = {b * 4, b * b * 4, N * b * b * 4};
+        if (!encode_map(&p.tmA0, q.rc_in, 2, dcoef, scoef, boxc, false) ||
+            !encode_map(&p.tmA1, q.ic_in, 2, dcoef, scoef, boxc, false) ||
+            !encode_map(&p.tmO, q.Fc, 4, dc, sc, box4, true))
+            return false;
+        p.a_chunk_bytes = 2 * 64 * kInvBox * sizeof(float);
+    }
+    return true;
+}
+
+// The tensor-map path is off for everything but the plain one-class BF16 launch at bw >= 64
+// (s2g_set_contraction_kernel(2) keeps the warp-specialised kernel on its cp.async path).
+static std::atomic<int> g_leg_tma{1};
+
+// Device table of the work items of one 64-function tile for tile N extent NB: order m has
+// 2 (parities) x nblk(m) (latitude blocks) x ceil(NP(m) / NB) (sub-blocks) items, orders in
+// increasing m (largest first); entry = (m, index of the item within its order).
+static int get_itab(Split* s, bool fwd, int NB, const int2** out, int* per_tile) {
     std::lock_guard<std::mutex> lk(g_split_mu);
     const int B = s->B;
-    std::vector<int> h(B + 1, 0);
+    std::vector<int2> h;
     for (int m = 0; m < B; ++m) {
         const Geo g = geo(fwd, B, m);
-        h[m + 1] = h[m] + 2 * g.nblk * ((g.NP + NB - 1) / NB);
+        const int n = 2 * g.nblk * ((g.NP + NB - 1) / NB);
+        for (int j = 0; j < n; ++j) h.push_back(make_int2(m, j));
     }
-    *per_tile = h[B];
-    for (auto& e : s->mstart[fwd])
+    *per_tile = (int)h.size();
+    for (auto& e : s->itab[fwd])
         if (e.first == NB) return (*out = e.second), S2G_OK;
-    int* d = nullptr;
-    S2G_CUDA(cudaMalloc(&d, sizeof(int) * (B + 1)));
-    const cudaError_t e = cudaMemcpy(d, h.data(), sizeof(int) * (B + 1), cudaMemcpyHostToDevice);
+    int2* d = nullptr;
+    S2G_CUDA(cudaMalloc(&d, sizeof(int2) * h.size()));
+    const cudaError_t e = cudaMemcpy(d, h.data(), sizeof(int2) * h.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(d);
         return cuda_fail(e, "cudaMemcpy");
     }
-    s->mstart[fwd].push_back({NB, d});
+    s->itab[fwd].push_back({NB, d});
     *out = d;
     return S2G_OK;
 }
@@ -1534,6 +1919,9 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     p.counter = counter;
     long long items = 0;
     int nbmax = 16;
+    // tensor-map TMA path: one class, BF16 terms, contiguous batches, bw >= 64, warp-specialised kernel
+    const bool want_tma = g_leg_tma && g_leg_kernel == 1 && !f16 && ncls == 1 && !spec[0].cmap &&
+                          spec[0].t->bw >= 64;
     for (int c = 0; c < ncls; ++c) {
         const LegSpec& q = spec[c];
         S2G_TRY(f16 ? build_split16(q.t) : build_split(q.t));
@@ -1542,11 +1930,13 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
         const int B = q.t->bw, npmax = leg_npmax(B, fwd);
         int NB = q.NB > 0 ? std::min(q.NB, npmax) : npmax;
         NB = std::max(16, std::min(256, NB) & ~15);  // the MMA's N is at most 256
+        // inverse TMA stores take 32-column blocks, and its staging leaves room for 128-row tables
+        if (want_tma && !fwd) NB = std::max(32, std::min(128, NB) & ~31);
         k.B = B;
         k.N = q.N;
         k.ntiles = (q.N + 63) / 64;
         k.NB = NB;
-        S2G_TRY(get_mstart(s, fwd, NB, &k.mstart, &k.per_tile));
+        S2G_TRY(get_itab(s, fwd, NB, &k.itab, &k.per_tile));
         k.item0 = items;
         k.tab_inv = f16 ? (float)(1.0 / s->tab16) : 1.f;
         k.C = q.C;
@@ -1566,6 +1956,7 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     }
     p.nitems = items;
     if (items == 0) return S2G_OK;
+    p.tma = want_tma && setup_tma(p, fwd, spec[0]) ? 1 : 0;
     if (items > 0x7fffffffLL) return fail(S2G_ERR_ARG, "contraction of %lld work items is too large", items);
     const int nt = f16 ? 2 : 3;
     if (g_leg_kernel == 1) return launch_leg_ws(fwd, f16, p, nbmax, items, counter, st);
@@ -1616,7 +2007,7 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
         smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + 2 * S + 2 * kWarps * PS);
         S2G_TRY(set_smem((const void*)k_dct_fwd_w<R>, smem));
         ProfScope ps_("dct_fwd_f32", st);
-        k_dct_fwd_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((const float*)in, (float*)out, nrows, s->w32,
+        k_dct_fwd_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((float*)in, (float*)out, nrows, s->w32,
                                                                         s->twS, s->twD);
     } else if (which == 2) {  // DCT-III
         smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + S + 2 * kWarps * PS);
@@ -1814,8 +2205,9 @@ __global__ void __launch_bounds__(128, 1) k_tc_selftest(int N, int K, int nprod,
 }  // namespace s2g
 
 extern "C" int s2g_set_contraction_kernel(int which) {
-    if (which != 0 && which != 1) return s2g::fail(S2G_ERR_ARG, "contraction kernel %d (0 or 1)", which);
-    s2g::g_leg_kernel = which;
+    if (which < 0 || which > 2) return s2g::fail(S2G_ERR_ARG, "contraction kernel %d (0, 1 or 2)", which);
+    s2g::g_leg_kernel = which == 0 ? 0 : 1;
+    s2g::g_leg_tma = which == 1 ? 1 : 0;
     return S2G_OK;
 }
 
