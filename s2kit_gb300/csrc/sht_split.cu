@@ -395,11 +395,14 @@ static int build_split16(Tables* t) {
 // Warp-FFT kernels (fft32.cuh), S = 2B = 32 R.  One warp owns one complex sequence; layout
 // changes go through padded shared memory.
 
-// Loads tw[k] = exp(2 pi i k / S), twD[k] = (cos, sin)(pi k / 2S) for k < S into shared memory.
-// (tw padded as padtw(k), see fft32.cuh; twD unpadded)
-__device__ __forceinline__ void load_tw(float2* tw, float2* twD, const float2* gS, const float2* gD, int S) {
+// Loads tw[k] = exp(2 pi i k / S) (padded as padtw(k)), its (register, lane) copy
+// twb[32 k1 + lane] = tw[(lane k1) mod S] for the warp FFT's stage (b) (see fft32.cuh), and
+// twD[k] = (cos, sin)(pi k / 2S) (unpadded, optional) for k < S into shared memory.
+__device__ __forceinline__ void load_tw(float2* tw, float2* twb, float2* twD, const float2* gS, const float2* gD,
+                                        int S) {
     for (int k = threadIdx.x; k < S; k += blockDim.x) {
         tw[padtw(k)] = gS[k];
+        twb[k] = gS[((k & 31) * (k >> 5)) & (S - 1)];
         if (twD) twD[k] = gD[k];
     }
 }
@@ -413,60 +416,78 @@ struct FftShape {
     static constexpr int T = 32 * W;
 };
 
-// DFT along phi of 16 latitudes (two real rows per warp), transposed to X[p][f][m][theta], m < B.
+// Shared-memory layouts of the FFT kernels put the 16-byte staged buffers first (per-warp
+// spectrum buffers padded to PSA floats, a multiple of 4) and the twiddle tables last.
+template <int R>
+struct FftSmem {
+    static constexpr int S = 32 * R, B = S / 2;
+    // per-warp spectrum stride: >= pad32(S), a multiple of 4, and 4 mod 32 so that the same
+    // element of different warps' spectra falls in different banks
+    static constexpr int PSA = (((S + S / 32) + 31) & ~31) + 4;
+    static constexpr int RS = B + B / 32 + 1;                    // padded transpose row (odd)
+    static constexpr int TILE = (FftShape<R>::LAT * RS + 3) & ~3; // one plane of the row kernels' tile
+    static constexpr int TS = FftShape<R>::LAT + 1;              // rows-inverse tile row (odd)
+    // the four-step warp FFT exchanges through the warp's spectrum rows
+    static_assert((R != 16 && R != 32) || R * (32 + 32 / R) <= PSA, "exchange planes fit the spectrum rows");
+};
+
+// DFT along phi of LAT latitudes (two real rows per warp), transposed to X[p][f][m][theta], m < B.
+// Each warp leaves its spectrum in shared memory; the separation of the two packed real rows,
+// X_a = (Z[m] + conj Z[S-m]) / 2 and X_b = (Z[m] - conj Z[S-m]) / 2i, is done by the threads
+// that write the transposed tile, each a float4 run of 4 latitudes of one order.
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N,
                                                     float scale, const float2* __restrict__ gtw,
                                                     const int64_t* __restrict__ gmap) {
-    constexpr int S = 32 * R, B = S / 2;
-    constexpr int PS = S + S / 32;        // padded spectrum length
-    constexpr int RS = B + B / 32 + 1;    // padded stage row (odd)
-    constexpr int TWL = twtab_len(S);
+    using L = FftSmem<R>;
+    constexpr int S = L::S, B = L::B, PSA = L::PSA;
+    constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
+    static_assert(S % LAT == 0 && LAT % 4 == 0, "row tiling");
     extern __shared__ __align__(16) float fsm[];
-    float2* tw = reinterpret_cast<float2*>(fsm);
-    float* spr = fsm + 2 * TWL;                    // [warps][PS] re
-    float* spi = spr + FftShape<R>::W * PS;                // [warps][PS] im
-    float* str = spi + FftShape<R>::W * PS;                // [16][RS] re
-    float* sti = str + FftShape<R>::LAT * RS;            // [16][RS] im
-    const int f = blockIdx.y, th0 = blockIdx.x * FftShape<R>::LAT;
+    float* spr = fsm;                  // [W][PSA] re
+    float* spi = spr + W * PSA;        // [W][PSA] im
+    float2* tw = reinterpret_cast<float2*>(spi + W * PSA);
+    float2* twb = tw + twtab_len(S);
+    const int f = blockIdx.y, th0 = blockIdx.x * LAT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    load_tw(tw, nullptr, gtw, nullptr, S);
+    load_tw(tw, twb, nullptr, gtw, nullptr, S);
     __syncthreads();
-    const int la = th0 + 2 * warp;
-    if (la < S) {
-        const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)la * S;
-        const float* rb = ra + S;
-        float2 v[R];
+    float2 v[R];
+    {
+        const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + 2 * warp) * S;
 #pragma unroll
-        for (int i = 0; i < R; ++i) v[i] = make_float2(ra[lane + 32 * i], (la + 1 < S) ? rb[lane + 32 * i] : 0.f);
-        WarpFFT<R>::run(v, tw, -1.f);
-        float* wr = spr + warp * PS;
-        float* wi = spi + warp * PS;
+        for (int i = 0; i < R; ++i) v[i] = make_float2(ra[lane + 32 * i], ra[S + lane + 32 * i]);
+    }
+    float* wr = spr + warp * PSA;
+    float* wi = spi + warp * PSA;
+    WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
 #pragma unroll
-        for (int k1 = 0; k1 < R; ++k1) {
-            const int o = pad32(WarpFFT<R>::out_index(k1));
-            wr[o] = v[k1].x;
-            wi[o] = v[k1].y;
-        }
-        __syncwarp();
-        for (int m = lane; m < B; m += 32) {
-            const int mm = (S - m) & (S - 1);
-            const float zr = wr[pad32(m)], zi = wi[pad32(m)], xr = wr[pad32(mm)], xi = wi[pad32(mm)];
-            str[(2 * warp) * RS + pad32(m)] = 0.5f * (zr + xr) * scale;
-            sti[(2 * warp) * RS + pad32(m)] = 0.5f * (zi - xi) * scale;
-            str[(2 * warp + 1) * RS + pad32(m)] = 0.5f * (zi + xi) * scale;
-            sti[(2 * warp + 1) * RS + pad32(m)] = -0.5f * (zr - xr) * scale;
-        }
+    for (int k1 = 0; k1 < R; ++k1) {
+        const int o = pad32(WarpFFTSel<R>::out_index(k1));
+        wr[o] = v[k1].x;
+        wi[o] = v[k1].y;
     }
     __syncthreads();
-    const int nlat = min(FftShape<R>::LAT, S - th0);
     const size_t plane = (size_t)N * B * S;
-    for (int e = threadIdx.x; e < B * FftShape<R>::LAT; e += blockDim.x) {
-        const int m = e / FftShape<R>::LAT, q = e - m * FftShape<R>::LAT;
-        if (q >= nlat) continue;
+    constexpr int Q4 = LAT / 4;
+    const float hs = 0.5f * scale;
+    for (int e = threadIdx.x; e < B * Q4; e += T) {
+        const int m = e / Q4, q = 4 * (e - m * Q4);
+        const int pm = pad32(m), pmm = pad32((S - m) & (S - 1));
+        float re[4], im[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {  // latitude pair q/2 + h is warp q/2 + h's (a, b) rows
+            const float* zr = spr + (q / 2 + h) * PSA;
+            const float* zi = spi + (q / 2 + h) * PSA;
+            const float ar = zr[pm], ai = zi[pm], br = zr[pmm], bi = zi[pmm];
+            re[2 * h] = (ar + br) * hs;
+            im[2 * h] = (ai - bi) * hs;
+            re[2 * h + 1] = (ai + bi) * hs;
+            im[2 * h + 1] = (br - ar) * hs;
+        }
         const size_t o = ((size_t)f * B + m) * S + th0 + q;
-        X[o] = str[q * RS + pad32(m)];
-        X[plane + o] = sti[q * RS + pad32(m)];
+        *reinterpret_cast<float4*>(X + o) = make_float4(re[0], re[1], re[2], re[3]);
+        *reinterpret_cast<float4*>(X + plane + o) = make_float4(im[0], im[1], im[2], im[3]);
     }
 }
 
@@ -474,48 +495,58 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
 // C[p][f][m][t][j] holds frequency k = 2j + t (j < B/2), so that the contraction's operand rows
 // of one parity are contiguous.  Naive orders are folded in place in X for their contraction:
 // X[p][f][m][t][j] = x[j] + (-1)^t x[S-1-j], j < B (the even/odd latitude halves).
+// Rows are read and written in 16-byte pieces through the warp's spectrum buffers.
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict__ X, float* __restrict__ Cout, int nrows,
                                                    const float* __restrict__ gw, const float2* __restrict__ gtw,
                                                    const float2* __restrict__ gtwD) {
-    constexpr int S = 32 * R, B = S / 2;
-    constexpr int PS = S + S / 32;
-    constexpr int TWL = twtab_len(S);
+    using L = FftSmem<R>;
+    constexpr int S = L::S, B = L::B, PSA = L::PSA;
+    constexpr int W = FftShape<R>::W;
     extern __shared__ __align__(16) float fsm[];
-    float2* tw = reinterpret_cast<float2*>(fsm);
-    float2* twD = tw + TWL;
-    float* w = fsm + 2 * TWL + 2 * S;    // 2S weights (even orders, then odd)
-    float* spr = w + 2 * S;
-    float* spi = spr + FftShape<R>::W * PS;
-    load_tw(tw, twD, gtw, gtwD, S);
+    float* spr = fsm;                  // [W][PSA]
+    float* spi = spr + W * PSA;        // [W][PSA]
+    float* w = spi + W * PSA;          // 2S weights (even orders, then odd)
+    float2* twP = reinterpret_cast<float2*>(w + 2 * S);  // B output twiddles, see below
+    float2* tw = twP + B;
+    float2* twb = tw + twtab_len(S);
+    load_tw(tw, twb, nullptr, gtw, nullptr, S);
+    // (cos, sin)(pi k / 2S) of output o (k = 2o, or 2(o - B/2) + 1 for o >= B/2), stored at
+    // (o % 4) B/4 + o / 4: the output loop's lanes (4 consecutive o each) read consecutive entries
+    for (int o = threadIdx.x; o < B; o += blockDim.x)
+        twP[(o & 3) * (B / 4) + (o >> 2)] = gtwD[o < B / 2 ? 2 * o : 2 * (o - B / 2) + 1];
     for (int q = threadIdx.x; q < 2 * S; q += blockDim.x) w[q] = gw[q];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * FftShape<R>::W + warp;
+    const int row = blockIdx.x * W + warp;
     if (row >= nrows) return;
     const int m = row % B;
+    float* xr = X + (size_t)row * S;
+    float* xi = xr + (size_t)nrows * S;
+    float* wr = spr + warp * PSA;
+    float* wi = spi + warp * PSA;
     if (naive_order(m)) {
-        float* xr = X + (size_t)row * S;
-        float* xi = xr + (size_t)nrows * S;
-        float* wr = spr + warp * PS;
-        float* wi = spi + warp * PS;
-        for (int q = lane; q < S; q += 32) {
-            wr[q] = xr[q];
-            wi[q] = xi[q];
+        for (int e = lane; e < S / 4; e += 32) {
+            reinterpret_cast<float4*>(wr)[e] = reinterpret_cast<const float4*>(xr)[e];
+            reinterpret_cast<float4*>(wi)[e] = reinterpret_cast<const float4*>(xi)[e];
         }
         __syncwarp();
-        for (int j = lane; j < B; j += 32) {
-            const float ar = wr[j], br = wr[S - 1 - j], ai = wi[j], bi = wi[S - 1 - j];
-            xr[j] = ar + br;
-            xr[B + j] = ar - br;
-            xi[j] = ai + bi;
-            xi[B + j] = ai - bi;
+        for (int e = lane; e < B / 4; e += 32) {
+            float a[4], b[4], c[4], d[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int j = 4 * e + u;
+                const float ar = wr[j], br = wr[S - 1 - j], ai = wi[j], bi = wi[S - 1 - j];
+                a[u] = ar + br, b[u] = ar - br, c[u] = ai + bi, d[u] = ai - bi;
+            }
+            reinterpret_cast<float4*>(xr)[e] = make_float4(a[0], a[1], a[2], a[3]);
+            reinterpret_cast<float4*>(xr + B)[e] = make_float4(b[0], b[1], b[2], b[3]);
+            reinterpret_cast<float4*>(xi)[e] = make_float4(c[0], c[1], c[2], c[3]);
+            reinterpret_cast<float4*>(xi + B)[e] = make_float4(d[0], d[1], d[2], d[3]);
         }
         return;
     }
     const float* ws = w + ((m & 1) ? S : 0);
-    const float* xr = X + (size_t)row * S;
-    const float* xi = xr + (size_t)nrows * S;
     float2 v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -523,12 +554,10 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
         const int q = (j < S / 2) ? 2 * j : 2 * (S - 1 - j) + 1;
         v[i] = make_float2(xr[q] * ws[q], xi[q] * ws[q]);
     }
-    WarpFFT<R>::run(v, tw, -1.f);
-    float* wr = spr + warp * PS;
-    float* wi = spi + warp * PS;
+    WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
 #pragma unroll
     for (int k1 = 0; k1 < R; ++k1) {
-        const int o = pad32(WarpFFT<R>::out_index(k1));
+        const int o = pad32(WarpFFTSel<R>::out_index(k1));
         wr[o] = v[k1].x;
         wi[o] = v[k1].y;
     }
@@ -541,42 +570,54 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
     // packed FFT's Hermitian halves do not cancel exactly in FP32, so store exact zeros (the
     // reference's REDFT10 of the zero imaginary row gives exact zeros, FST_semi_memo.c:96-120).
     const bool im_zero = (m == 0);
-    for (int k = lane; k < B; k += 32) {
-        const int kk = (S - k) & (S - 1);
-        const float ar = wr[pad32(k)], ai = wi[pad32(k)], br = wr[pad32(kk)], bi = wi[pad32(kk)];
-        const float c = twD[k].x, sn = twD[k].y;
-        const float fct = (k == 0) ? nrm0 : nrm;
-        const int o = (k & 1) * (B / 2) + (k >> 1);
-        cr[o] = ((ar + br) * c + (ai - bi) * sn) * fct;
-        ci[o] = im_zero ? 0.f : ((ai + bi) * c - (ar - br) * sn) * fct;
+    for (int e = lane; e < B / 4; e += 32) {
+        float a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int o = 4 * e + u;                         // o = (k & 1) * B/2 + k/2
+            const int k = o < B / 2 ? 2 * o : 2 * (o - B / 2) + 1;
+            const int kk = (S - k) & (S - 1);
+            const float ar = wr[pad32(k)], ai = wi[pad32(k)], br = wr[pad32(kk)], bi = wi[pad32(kk)];
+            const float2 cs = twP[u * (B / 4) + e];
+            const float c = cs.x, sn = cs.y;
+            const float fct = (k == 0) ? nrm0 : nrm;
+            a[u] = ((ar + br) * c + (ai - bi) * sn) * fct;
+            b[u] = im_zero ? 0.f : ((ai + bi) * c - (ar - br) * sn) * fct;
+        }
+        reinterpret_cast<float4*>(cr)[e] = make_float4(a[0], a[1], a[2], a[3]);
+        reinterpret_cast<float4*>(ci)[e] = make_float4(b[0], b[1], b[2], b[3]);
     }
 }
 
 // REDFT01 per (function, seminaive order) row, sin(theta) for odd m, scale: F[p][f][m][theta].
+// Rows are read and written in 16-byte pieces through the warp's spectrum buffers.
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
                                                    const float* __restrict__ gsin, const float2* __restrict__ gtw,
                                                    const float2* __restrict__ gtwD, float scale) {
-    constexpr int S = 32 * R, B = S / 2;
-    constexpr int PS = S + S / 32;
-    constexpr int TWL = twtab_len(S);
+    using L = FftSmem<R>;
+    constexpr int S = L::S, B = L::B, PSA = L::PSA;
+    constexpr int W = FftShape<R>::W;
     extern __shared__ __align__(16) float fsm[];
-    float2* tw = reinterpret_cast<float2*>(fsm);
-    float2* twD = tw + TWL;
-    float* sn = fsm + 2 * TWL + 2 * S;
-    float* spr = sn + S;
-    float* spi = spr + FftShape<R>::W * PS;
-    load_tw(tw, twD, gtw, gtwD, S);
+    float* spr = fsm;                  // [W][PSA]
+    float* spi = spr + W * PSA;        // [W][PSA]
+    float* sn = spi + W * PSA;         // S
+    float2* twD = reinterpret_cast<float2*>(sn + S);
+    float2* tw = twD + S;
+    float2* twb = tw + twtab_len(S);
+    load_tw(tw, twb, twD, gtw, gtwD, S);
     for (int q = threadIdx.x; q < S; q += blockDim.x) sn[q] = gsin[q];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * FftShape<R>::W + warp;
+    const int row = blockIdx.x * W + warp;
     if (row >= nrows) return;
     const int m = row % B;
     if (naive_order(m)) return;
+    float* zr = spr + warp * PSA;
+    float* zi = spi + warp * PSA;
     // Fc[p][f][m][t][j]: cosine coefficient k = 2j + t at (k & 1) * B/2 + k/2
     const float* xa = Fc + (size_t)row * B;
-    const float* xb = xa + (size_t)nrows * B;
+    const float* xb = Fc + (size_t)(nrows + row) * B;
     float2 v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -589,12 +630,10 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
         const float2 d = twD[k];
         v[i] = make_float2(wr * d.x - wi * d.y, wr * d.y + wi * d.x);
     }
-    WarpFFT<R>::run(v, tw, 1.f);
-    float* zr = spr + warp * PS;
-    float* zi = spi + warp * PS;
+    WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
 #pragma unroll
     for (int k1 = 0; k1 < R; ++k1) {
-        const int o = pad32(WarpFFT<R>::out_index(k1));
+        const int o = pad32(WarpFFTSel<R>::out_index(k1));
         zr[o] = v[k1].x;
         zi[o] = v[k1].y;
     }
@@ -602,43 +641,60 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     float* fr = F + (size_t)row * S;
     float* fi = fr + (size_t)nrows * S;
     const bool odd = m & 1;
-    for (int q = lane; q < S; q += 32) {
-        const int src = (q & 1) ? S - 1 - (q >> 1) : (q >> 1);
-        const float g = odd ? sn[q] * scale : scale;
-        fr[q] = zr[pad32(src)] * g;
-        fi[q] = zi[pad32(src)] * g;
+    for (int e = lane; e < S / 4; e += 32) {
+        float a[4], b[4];
+        const float4 s4 = reinterpret_cast<const float4*>(sn)[e];
+        const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = 4 * e + u;
+            const int src = (q & 1) ? S - 1 - (q >> 1) : (q >> 1);
+            const float g = odd ? sv[u] * scale : scale;
+            a[u] = zr[pad32(src)] * g;
+            b[u] = zi[pad32(src)] * g;
+        }
+        reinterpret_cast<float4*>(fr)[e] = make_float4(a[0], a[1], a[2], a[3]);
+        reinterpret_cast<float4*>(fi)[e] = make_float4(b[0], b[1], b[2], b[3]);
     }
 }
 
-// DFT with sign +1 over the orders for 16 latitudes (two real output rows per warp).
+// DFT with sign +1 over the orders for LAT latitudes (two real output rows per warp).  The
+// order-major input arrives as float4 runs of 4 latitudes; output rows leave as float4.
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
                                                     const float2* __restrict__ gtw,
                                                     const int64_t* __restrict__ gmap) {
-    constexpr int S = 32 * R, B = S / 2;
-    constexpr int PS = S + S / 32;
-    constexpr int TS = FftShape<R>::LAT + 1;  // padded tile row (odd)
-    constexpr int TWL = twtab_len(S);
+    using L = FftSmem<R>;
+    constexpr int S = L::S, B = L::B, PSA = L::PSA, TS = L::TS;
+    constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
+    static_assert(S % LAT == 0 && LAT % 4 == 0 && (B * TS) % 4 == 0, "row staging");
     extern __shared__ __align__(16) float fsm[];
-    float2* tw = reinterpret_cast<float2*>(fsm);
-    float* tr = fsm + 2 * TWL;           // [B][TS]
+    // the order-major tile [B][TS] (re, im) is dead once every warp holds its inputs; the warps'
+    // spectrum buffers [W][PSA] (re, im) then reuse the same space
+    constexpr int U = 2 * B * TS > 2 * W * PSA ? 2 * B * TS : 2 * W * PSA;
+    float* tr = fsm;
     float* ti = tr + B * TS;
-    float* spr = ti + B * TS;            // [warps][PS]
-    float* spi = spr + FftShape<R>::W * PS;
-    const int f = blockIdx.y, th0 = blockIdx.x * FftShape<R>::LAT;
+    float* spr = fsm;
+    float* spi = spr + W * PSA;
+    float2* tw = reinterpret_cast<float2*>(fsm + U);
+    float2* twb = tw + twtab_len(S);
+    const int f = blockIdx.y, th0 = blockIdx.x * LAT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    load_tw(tw, nullptr, gtw, nullptr, S);
-    const int nlat = min(FftShape<R>::LAT, S - th0);
+    load_tw(tw, twb, nullptr, gtw, nullptr, S);
     const size_t plane = (size_t)N * B * S;
-    for (int e = threadIdx.x; e < B * FftShape<R>::LAT; e += blockDim.x) {
-        const int m = e / FftShape<R>::LAT, q = e - m * FftShape<R>::LAT;
+    constexpr int Q4 = LAT / 4;
+    for (int e = threadIdx.x; e < B * Q4; e += T) {
+        const int m = e / Q4, q = 4 * (e - m * Q4);
         const size_t o = ((size_t)f * B + m) * S + th0 + q;
-        tr[m * TS + q] = (q < nlat) ? F[o] : 0.f;
-        ti[m * TS + q] = (q < nlat) ? F[plane + o] : 0.f;
+        const float4 a = *reinterpret_cast<const float4*>(F + o);
+        const float4 b = *reinterpret_cast<const float4*>(F + plane + o);
+        float* pr = tr + m * TS + q;
+        float* pi = ti + m * TS + q;
+        pr[0] = a.x, pr[1] = a.y, pr[2] = a.z, pr[3] = a.w;
+        pi[0] = b.x, pi[1] = b.y, pi[2] = b.z, pi[3] = b.w;
     }
     __syncthreads();
     const int a = 2 * warp, b = a + 1;
-    if (th0 + a >= S) return;
     float2 v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -658,20 +714,24 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
         }
         v[i] = make_float2(ar - bi, ai + br);  // F_a + i F_b
     }
-    WarpFFT<R>::run(v, tw, 1.f);
-    float* zr = spr + warp * PS;
-    float* zi = spi + warp * PS;
+    __syncthreads();  // the tile is dead: spectrum buffers below overwrite it
+    float* zr = spr + warp * PSA;
+    float* zi = spi + warp * PSA;
+    WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
 #pragma unroll
     for (int k1 = 0; k1 < R; ++k1) {
-        const int o = pad32(WarpFFT<R>::out_index(k1));
+        const int o = pad32(WarpFFTSel<R>::out_index(k1));
         zr[o] = v[k1].x;
         zi[o] = v[k1].y;
     }
     __syncwarp();
     float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;
-    for (int k = lane; k < S; k += 32) {
-        ga[k] = zr[pad32(k)];
-        if (th0 + b < S) ga[S + k] = zi[pad32(k)];
+    for (int e = lane; e < S / 4; e += 32) {
+        const int k = 4 * e;
+        reinterpret_cast<float4*>(ga)[e] =
+            make_float4(zr[pad32(k)], zr[pad32(k + 1)], zr[pad32(k + 2)], zr[pad32(k + 3)]);
+        reinterpret_cast<float4*>(ga + S)[e] =
+            make_float4(zi[pad32(k)], zi[pad32(k + 1)], zi[pad32(k + 2)], zi[pad32(k + 3)]);
     }
 }
 
@@ -1993,32 +2053,33 @@ template <int R>
 static int launch_fft_kernels(int which, const void* in, void* out, int N, const Split* s, cudaStream_t st,
                               float scale, const int64_t* gmap) {
     constexpr int S = 32 * R, B = S / 2;
-    constexpr int PS = S + S / 32;
     constexpr int kWarps = FftShape<R>::W, kLatPerCta = FftShape<R>::LAT, kThreads = FftShape<R>::T;
     const int nrows = N * B;
     size_t smem = 0;
+    using L = FftSmem<R>;
+    const size_t tw_bytes = sizeof(float2) * (twtab_len(S) + S), spec = sizeof(float) * 2 * kWarps * L::PSA;
     if (which == 0) {  // rows forward
-        smem = sizeof(float) * (2 * twtab_len(S) + 2 * kWarps * PS + 2 * kLatPerCta * (B + B / 32 + 1));
+        smem = spec + tw_bytes;
         S2G_TRY(set_smem((const void*)k_rows_fwd_w<R>, smem));
-        dim3 g((S + kLatPerCta - 1) / kLatPerCta, N);
+        dim3 g(S / kLatPerCta, N);
         ProfScope ps_("rows_fwd_f32", st);
         k_rows_fwd_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, N, scale, s->twS, gmap);
     } else if (which == 1) {  // DCT-II
-        smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + 2 * S + 2 * kWarps * PS);
+        smem = spec + sizeof(float) * 2 * S + sizeof(float2) * B + tw_bytes;
         S2G_TRY(set_smem((const void*)k_dct_fwd_w<R>, smem));
         ProfScope ps_("dct_fwd_f32", st);
         k_dct_fwd_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((float*)in, (float*)out, nrows, s->w32,
                                                                         s->twS, s->twD);
     } else if (which == 2) {  // DCT-III
-        smem = sizeof(float) * (2 * twtab_len(S) + 2 * S + S + 2 * kWarps * PS);
+        smem = spec + sizeof(float) * S + sizeof(float2) * S + tw_bytes;
         S2G_TRY(set_smem((const void*)k_dct_inv_w<R>, smem));
         ProfScope ps_("dct_inv_f32", st);
         k_dct_inv_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((const float*)in, (float*)out, nrows,
                                                                         s->sin32, s->twS, s->twD, scale);
     } else {  // rows inverse
-        smem = sizeof(float) * (2 * twtab_len(S) + 2 * B * (kLatPerCta + 1) + 2 * kWarps * PS);
+        smem = std::max(sizeof(float) * 2 * B * L::TS, spec) + tw_bytes;
         S2G_TRY(set_smem((const void*)k_rows_inv_w<R>, smem));
-        dim3 g((S + kLatPerCta - 1) / kLatPerCta, N);
+        dim3 g(S / kLatPerCta, N);
         ProfScope ps_("rows_inv_f32", st);
         k_rows_inv_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, N, s->twS, gmap);
     }
