@@ -683,15 +683,31 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
     load_tw(tw, twb, nullptr, gtw, nullptr, S);
     const size_t plane = (size_t)N * B * S;
     constexpr int Q4 = LAT / 4;
-    for (int e = threadIdx.x; e < B * Q4; e += T) {
-        const int m = e / Q4, q = 4 * (e - m * Q4);
-        const size_t o = ((size_t)f * B + m) * S + th0 + q;
-        const float4 a = *reinterpret_cast<const float4*>(F + o);
-        const float4 b = *reinterpret_cast<const float4*>(F + plane + o);
-        float* pr = tr + m * TS + q;
-        float* pi = ti + m * TS + q;
-        pr[0] = a.x, pr[1] = a.y, pr[2] = a.z, pr[3] = a.w;
-        pi[0] = b.x, pi[1] = b.y, pi[2] = b.z, pi[3] = b.w;
+    // loads of up to four iterations are issued before their shared-memory stores
+    constexpr int NIT = (B * Q4 + T - 1) / T, BAT = NIT < 4 ? NIT : 4;
+    for (int it0 = 0; it0 < NIT; it0 += BAT) {
+        float4 a[BAT], b[BAT];
+#pragma unroll
+        for (int u = 0; u < BAT; ++u) {
+            const int e = threadIdx.x + (it0 + u) * T;
+            if (e < B * Q4) {
+                const int m = e / Q4, q = 4 * (e - m * Q4);
+                const size_t o = ((size_t)f * B + m) * S + th0 + q;
+                a[u] = *reinterpret_cast<const float4*>(F + o);
+                b[u] = *reinterpret_cast<const float4*>(F + plane + o);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < BAT; ++u) {
+            const int e = threadIdx.x + (it0 + u) * T;
+            if (e < B * Q4) {
+                const int m = e / Q4, q = 4 * (e - m * Q4);
+                float* pr = tr + m * TS + q;
+                float* pi = ti + m * TS + q;
+                pr[0] = a[u].x, pr[1] = a[u].y, pr[2] = a[u].z, pr[3] = a[u].w;
+                pi[0] = b[u].x, pi[1] = b[u].y, pi[2] = b[u].z, pi[3] = b[u].w;
+            }
+        }
     }
     __syncthreads();
     const int a = 2 * warp, b = a + 1;
