@@ -895,7 +895,7 @@ static int host_pipeline(s2g_plan p, int fwd, const float* in0, const float* in1
     S2G_TRY(plan_check(p, batch));
     const size_t S = 2 * (size_t)p->bw, ng = S * S, nc = (size_t)p->bw * p->bw;
     const size_t in_per = fwd ? ng : 2 * nc, out_per = fwd ? 2 * nc : ng;
-    int chunk = batch < 64 ? batch : 64;
+    int chunk = batch < 32 ? batch : 32;  // short fill and drain: the first upload and last download do not overlap
     while (chunk > 1 && (size_t)chunk * (in_per + out_per) * 4 * 2 > ((size_t)4 << 30)) chunk /= 2;
     const size_t in_b = (size_t)chunk * in_per * 4, out_b = (size_t)chunk * out_per * 4;
     S2G_TRY(p->io.ensure(2 * (in_b + out_b) + 1024));

@@ -885,6 +885,16 @@ __device__ __forceinline__ void load_seg(const LegClass& k, int m, bool nv, int 
     }
 }
 
+// Task q of producer thread tid: A-tile row r (function f0 + r % 64, plane r / 64) and 8-column
+// segment seg of the chunk.  Eight consecutive lanes take the eight rows of one core matrix (one
+// contiguous 128-byte block of the tile), so each quarter-warp's 16-byte shared-memory stores hit
+// 32 distinct banks; the four tasks of a row (seg 0..3) are lanes l, l + 8, l + 16, l + 24.
+__device__ __forceinline__ void task_rs(int tid, int q, int& r, int& seg) {
+    const int lane = tid & 31;
+    seg = lane >> 3;
+    r = q * 64 + (tid >> 5) * 8 + (lane & 7);
+}
+
 // A operand of one chunk, split into loads (issued early, held in registers across the
 // barrier and the MMA issue of the previous chunk) and the split + shared-memory store.
 static constexpr int kTasks = 128 * (kKC / 8) / kTPB;  // (row, 8-column segment) tasks per thread
@@ -892,11 +902,10 @@ static constexpr int kTasks = 128 * (kKC / 8) / kTPB;  // (row, 8-column segment
 template <bool FWD>
 __device__ __forceinline__ void load_a(const LegClass& k, int m, bool nv, int t, int f0, int c,
                                        float (&v)[kTasks][8], int tid) {
-    constexpr int segs = kKC / 8;
 #pragma unroll
     for (int q = 0; q < kTasks; ++q) {
-        const int task = tid + q * kTPB;
-        const int r = task / segs, seg = task - r * segs;
+        int r, seg;
+        task_rs(tid, q, r, seg);
         load_seg<FWD>(k, m, nv, t, f0 + (r & 63), r >> 6, c, seg, v[q]);
     }
 }
@@ -923,11 +932,10 @@ __device__ __forceinline__ void split_terms(float x, uint16_t& h0, uint16_t& h1,
 template <bool F16>
 __device__ __forceinline__ void store_a(uint8_t* st, const float (&v)[kTasks][8], const float (&sc)[kTasks],
                                         int tid) {
-    constexpr int segs = kKC / 8;
 #pragma unroll
     for (int q = 0; q < kTasks; ++q) {
-        const int task = tid + q * kTPB;
-        const int r = task / segs, seg = task - r * segs;
+        int r, seg;
+        task_rs(tid, q, r, seg);
         uint32_t w[3][4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -1107,14 +1115,15 @@ __global__ void __launch_bounds__(kTPB, 2) k_leg_tc(Leg p, uint32_t stage_bytes,
             }
 #pragma unroll
             for (int q = 0; q < kTasks; ++q) {
-                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 1));
-                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 2));
+                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 8));
+                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 16));
                 int e = 0;
                 frexpf(mx[q], &e);  // mx < 2^e
                 const int sh = mx[q] > 0.f ? min(14 - e, 120) : 0;
                 sc[q] = ldexpf(1.f, sh);
-                const int task = threadIdx.x + q * kTPB;
-                if ((task & 3) == 0) s_rinv[task >> 2] = ldexpf(1.f, -sh);
+                int r, seg;
+                task_rs(threadIdx.x, q, r, seg);
+                if (seg == 0) s_rinv[r] = ldexpf(1.f, -sh);
             }
         } else {
 #pragma unroll
@@ -1265,11 +1274,10 @@ template <bool FWD>
 __device__ __forceinline__ void issue_chunk(const LegClass& K, const WsItem& e, int c, float4* stg, int s, int tid) {
     const int B = K.B;
     const bool nv = FWD && naive_order(e.m);
-    constexpr int segs = kKC / 8;
 #pragma unroll
     for (int q = 0; q < kTasks; ++q) {
-        const int task = tid + q * kAProd;
-        const int r = task / segs, seg = task - r * segs;
+        int r, seg;
+        task_rs(tid, q, r, seg);
         const int f = e.f0 + (r & 63), part = r >> 6;
         const int j0 = c * kKC + seg * 8;
         float4* d0 = stg_at(stg, s, q, 0, tid);
@@ -1393,7 +1401,6 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
                                               uint64_t* stg_full, uint64_t* stg_empty, uint64_t* a_full,
                                               uint64_t* a_empty, volatile int* s_abort, int tid) {
     constexpr uint32_t kAStage = 3 * kATile;
-    constexpr int segs = kKC / 8;
     const unsigned full = 0xffffffffu;
     uint32_t ac = 0, sc = 0;  // A tiles produced, staging chunks consumed
     float one[kTasks];
@@ -1424,8 +1431,8 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
             float va[kTasks][8];
 #pragma unroll
             for (int q = 0; q < kTasks; ++q) {
-                const int task = tid + q * kAProd;
-                const int r = task / segs, seg = task - r * segs;
+                int r, seg;
+                task_rs(tid, q, r, seg);
                 const int j0 = c * kKC + seg * 8;
                 if (FWD) {
                     // 128-byte rows (p, f), 16-byte chunk u of row r stored at chunk u ^ (r % 8)
@@ -1762,14 +1769,15 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 }
 #pragma unroll
                 for (int q = 0; q < kTasks; ++q) {
-                    mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 1));
-                    mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 2));
+                    mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 8));
+                    mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 16));
                     int ex = 0;
                     frexpf(mx[q], &ex);  // mx < 2^ex
                     const int sh = mx[q] > 0.f ? min(14 - ex, 120) : 0;
                     sc[q] = ldexpf(1.f, sh);
-                    const int task = tid + q * kTPB;
-                    if ((task & 3) == 0) s_rinv[slot][task >> 2] = ldexpf(1.f, -sh);
+                    int r, seg;
+                    task_rs(tid, q, r, seg);
+                    if (seg == 0) s_rinv[slot][r] = ldexpf(1.f, -sh);
                 }
                 tc::mbar_arrive(&sc_full[slot]);
             } else {
