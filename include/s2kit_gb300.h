@@ -2,7 +2,7 @@
  * s2kit_gb300.h -- C ABI of the GB300 (sm_103a) seminaive spherical harmonic transform library.
  *
  * Part 1 is a drop-in for S2kit 1.1's memo path: every function keeps the reference
- * signature (include/s2kit/*.h), argument meaning and coefficient layout, takes HOST
+ * signature (the headers in include/s2kit/), argument meaning and coefficient layout, takes HOST
  * buffers, and runs on the GPU (CUDA device 0 unless S2G_DEVICE selects another).
  * FFTW plans are accepted and ignored (NULL is fine).  Tables produced by the table
  * builders below are generated on the GPU and copied into the caller's buffers.
@@ -63,6 +63,21 @@ void FZTSemiMemo(double* rdata, double* idata, double* rres, double* ires, const
  * on every call); workspace is unused. */
 void ConvOn2SphereSemiMemo(double* rdata, double* idata, double* rfilter, double* ifilter, double* rres,
                            double* ires, const int bw, double* workspace);
+
+/* Replace the on-the-fly family, src/FST_semi_fly.c (include/s2kit/FST_semi_fly.h:8-16):
+ * FSTSemiFly :67-211, InvFSTSemiFly :235-369, FZTSemiFly :390-425, ConvOn2SphereSemiFly :454-519.
+ * The reference generates each order's Legendre table inside every call; here the tables for
+ * (bw, cutoff) are generated on the GPU on first use and kept, and the transforms are those of
+ * the memo family above.  Workspace and plans are ignored; weights are used when given. */
+void FSTSemiFly(double* rdata, double* idata, double* rcoeffs, double* icoeffs, const int bw, double* workspace,
+                DataFormat data_format, const int cutoff, fftw_plan* DCT_plan, fftw_plan* FFT_plan,
+                double* weights);
+void InvFSTSemiFly(double* rcoeffs, double* icoeffs, double* rdata, double* idata, const int bw, double* workspace,
+                   DataFormat data_format, const int cutoff, fftw_plan* inv_DCT_plan, fftw_plan* inv_FFT_plan);
+void FZTSemiFly(double* rdata, double* idata, double* rres, double* ires, const int bw, double* workspace,
+                DataFormat data_format, fftw_plan* DCT_plan, double* weights);
+void ConvOn2SphereSemiFly(double* rdata, double* idata, double* rfilter, double* ifilter, double* rres,
+                          double* ires, const int bw, double* workspace);
 
 /* Replaces DLTSemi, src/legendre_transform/seminaive.c:153-198 (seminaive.h:6). */
 void DLTSemi(double* data, const int bw, const int m, double* result, double* workspace, double* cos_pml_table,

@@ -290,6 +290,13 @@ class Reference:
         L.ConvOn2SphereSemiMemo.argtypes = [_dp] * 6 + [C.c_int, _dp]
         L.TransMult.argtypes = [_dp] * 6 + [C.c_int]
         L.DLTSemi.argtypes = [_dp, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(vp)]
+        # on-the-fly family (src/FST_semi_fly.c): tables generated per order inside each call
+        L.FSTSemiFly.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, C.c_int, C.c_int, C.POINTER(vp), C.POINTER(vp),
+                                 _dp]
+        L.InvFSTSemiFly.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, C.c_int, C.c_int, C.POINTER(vp),
+                                    C.POINTER(vp)]
+        L.FZTSemiFly.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, C.c_int, C.POINTER(vp), _dp]
+        L.ConvOn2SphereSemiFly.argtypes = [_dp] * 6 + [C.c_int, _dp]
         L.InvDLTSemi.argtypes = [_dp, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(vp)]
         self._keep = []
 
@@ -370,6 +377,50 @@ class Reference:
         self.lib.FZTSemiMemo(_ptr(rdata), _ptr(idata), _ptr(rr), _ptr(ii), bw, tf[0], _ptr(ws), data_format,
                              C.byref(dct), _ptr(w))
         return rr[:bw], ii
+
+    # ---- on-the-fly family: workspace sizes as documented at FST_semi_fly.c:58, 225, 447.  FZTSemiFly
+    # documents 12*bw (:383) but uses 4*bw + 2*bw*bw (:394-397) plus GenerateCosPmlTable's 9*bw
+    # (cospml.c:143), i.e. 2*bw*bw + 13*bw; the documented size corrupts the heap, so more is passed
+    def fst_fly(self, rdata, idata, bw, data_format=REAL, cutoff=None):
+        cutoff = bw if cutoff is None else cutoff
+        dct, _, fft, _ = self._plans(bw)
+        w = self.weights(bw)
+        rdata = np.array(rdata, dtype=np.float64).reshape(-1)
+        idata = np.array(idata, dtype=np.float64).reshape(-1)
+        rc, ic = np.zeros(bw * bw), np.zeros(bw * bw)
+        ws = np.zeros(10 * bw * bw + 24 * bw)
+        self.lib.FSTSemiFly(_ptr(rdata), _ptr(idata), _ptr(rc), _ptr(ic), bw, _ptr(ws), data_format, cutoff,
+                            C.byref(dct), C.byref(fft), _ptr(w))
+        return rc, ic
+
+    def inv_fst_fly(self, rcoeffs, icoeffs, bw, data_format=REAL, cutoff=None):
+        cutoff = bw if cutoff is None else cutoff
+        _, idct, _, ifft = self._plans(bw)
+        rc = np.array(rcoeffs, dtype=np.float64)
+        ic = np.array(icoeffs, dtype=np.float64)
+        rd, idd = np.zeros(4 * bw * bw), np.zeros(4 * bw * bw)
+        ws = np.zeros(10 * bw * bw + 24 * bw)
+        self.lib.InvFSTSemiFly(_ptr(rc), _ptr(ic), _ptr(rd), _ptr(idd), bw, _ptr(ws), data_format, cutoff,
+                               C.byref(idct), C.byref(ifft))
+        return rd, idd
+
+    def fzt_fly(self, rdata, idata, bw, data_format=REAL):
+        dct, _, _, _ = self._plans(bw)
+        w = self.weights(bw)
+        rdata = np.array(rdata, dtype=np.float64).reshape(-1)
+        idata = np.array(idata, dtype=np.float64).reshape(-1)
+        rr, ii = np.zeros(2 * bw), np.zeros(2 * bw)
+        ws = np.zeros(2 * bw * bw + 16 * bw)
+        self.lib.FZTSemiFly(_ptr(rdata), _ptr(idata), _ptr(rr), _ptr(ii), bw, _ptr(ws), data_format, C.byref(dct),
+                            _ptr(w))
+        return rr[:bw], ii
+
+    def conv_fly(self, rdata, idata, rfilter, ifilter, bw):
+        args = [np.array(a, dtype=np.float64).reshape(-1) for a in (rdata, idata, rfilter, ifilter)]
+        rr, ir = np.zeros(4 * bw * bw), np.zeros(4 * bw * bw)
+        ws = np.zeros(14 * bw * bw + 26 * bw)
+        self.lib.ConvOn2SphereSemiFly(*[_ptr(a) for a in args], _ptr(rr), _ptr(ir), bw, _ptr(ws))
+        return rr, ir
 
     def conv(self, rdata, idata, rfilter, ifilter, bw):
         L = self.lib

@@ -23,6 +23,10 @@ SIGNATURES = {
     "InvFSTSemiMemo": (None, [dp, dp, dp, dp, C.c_int, dpp, dp, C.c_int, C.c_int, vp, vp]),
     "FZTSemiMemo": (None, [dp, dp, dp, dp, C.c_int, dp, dp, C.c_int, vp, dp]),
     "ConvOn2SphereSemiMemo": (None, [dp, dp, dp, dp, dp, dp, C.c_int, dp]),
+    "FSTSemiFly": (None, [dp, dp, dp, dp, C.c_int, dp, C.c_int, C.c_int, vp, vp, dp]),
+    "InvFSTSemiFly": (None, [dp, dp, dp, dp, C.c_int, dp, C.c_int, C.c_int, vp, vp]),
+    "FZTSemiFly": (None, [dp, dp, dp, dp, C.c_int, dp, C.c_int, vp, dp]),
+    "ConvOn2SphereSemiFly": (None, [dp, dp, dp, dp, dp, dp, C.c_int, dp]),
     "DLTSemi": (None, [dp, C.c_int, C.c_int, dp, dp, dp, dp, vp]),
     "InvDLTSemi": (None, [dp, C.c_int, C.c_int, dp, dp, dp, dp, vp]),
     "DLTNaive": (None, [dp, C.c_int, C.c_int, dp, dp, dp, dp]),

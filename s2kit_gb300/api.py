@@ -126,6 +126,28 @@ def ConvOn2SphereSemiMemo(rdata, idata, rfilter, ifilter, rres, ires, bw, worksp
                                  _p(workspace))
 
 
+# On-the-fly family (src/FST_semi_fly.c): same arguments as the reference, no table argument.
+def FSTSemiFly(rdata, idata, rcoeffs, icoeffs, bw, workspace, data_format, cutoff, DCT_plan=None, FFT_plan=None,
+               weights=None):
+    load().FSTSemiFly(_p(rdata), _p(idata), _p(rcoeffs), _p(icoeffs), bw, _p(workspace), data_format, cutoff, None,
+                      None, _p(weights))
+
+
+def InvFSTSemiFly(rcoeffs, icoeffs, rdata, idata, bw, workspace, data_format, cutoff, inv_DCT_plan=None,
+                  inv_FFT_plan=None):
+    load().InvFSTSemiFly(_p(rcoeffs), _p(icoeffs), _p(rdata), _p(idata), bw, _p(workspace), data_format, cutoff,
+                         None, None)
+
+
+def FZTSemiFly(rdata, idata, rres, ires, bw, workspace, data_format, DCT_plan=None, weights=None):
+    load().FZTSemiFly(_p(rdata), _p(idata), _p(rres), _p(ires), bw, _p(workspace), data_format, None, _p(weights))
+
+
+def ConvOn2SphereSemiFly(rdata, idata, rfilter, ifilter, rres, ires, bw, workspace=None):
+    load().ConvOn2SphereSemiFly(_p(rdata), _p(idata), _p(rfilter), _p(ifilter), _p(rres), _p(ires), bw,
+                                _p(workspace))
+
+
 def DLTSemi(data, bw, m, result, workspace, cos_pml_table, weights, plan=None):
     load().DLTSemi(_p(data), bw, m, _p(result), _p(workspace), _p(cos_pml_table), _p(weights), None)
 

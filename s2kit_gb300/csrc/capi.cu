@@ -302,14 +302,14 @@ static int do_fst(double* rdata, double* idata, double* rcoeffs, double* icoeffs
                   int fmt, int cutoff, double* weights) {
     S2G_TRY(check_bw(bw));
     S2G_TRY(check_cutoff(bw, cutoff));
-    if (!rdata || !idata || !rcoeffs || !icoeffs || !table) return fail(S2G_ERR_ARG, "NULL argument");
+    if (!rdata || !idata || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(dropin_device());
     Tables* base;
     S2G_TRY(get_tables(bw, cutoff, &base));
     TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
-    S2G_TRY(upload_table(base, table, 0, &view.fwd));
+    if (table) S2G_TRY(upload_table(base, table, 0, &view.fwd));  // null: the device's own table (on the fly)
     const size_t S = 2 * (size_t)bw, ng = S * S, nc = (size_t)bw * bw;
     const size_t need = 2 * rnd(ng) + 2 * rnd(nc) + rnd(4 * (size_t)bw) + f64_work_bytes(bw, 1, fmt) + 256;
     S2G_TRY(g_dscratch.s.ensure(need));
@@ -332,14 +332,14 @@ static int do_inv_fst(double* rcoeffs, double* icoeffs, double* rdata, double* i
                       int fmt, int cutoff) {
     S2G_TRY(check_bw(bw));
     S2G_TRY(check_cutoff(bw, cutoff));
-    if (!rdata || !idata || !rcoeffs || !icoeffs || !ttable) return fail(S2G_ERR_ARG, "NULL argument");
+    if (!rdata || !idata || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(dropin_device());
     Tables* base;
     S2G_TRY(get_tables(bw, cutoff, &base));
     TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
-    S2G_TRY(upload_table(base, ttable, 1, &view.inv));
+    if (ttable) S2G_TRY(upload_table(base, ttable, 1, &view.inv));  // null: the device's own table
     const size_t S = 2 * (size_t)bw, ng = S * S, nc = (size_t)bw * bw;
     const size_t need = 2 * rnd(ng) + 2 * rnd(nc) + f64_work_bytes(bw, 1, fmt) + 256;
     S2G_TRY(g_dscratch.s.ensure(need));
@@ -357,7 +357,7 @@ static int do_inv_fst(double* rcoeffs, double* icoeffs, double* rdata, double* i
 static int do_fzt(double* rdata, double* idata, double* rres, double* ires, int bw, double* cos_pml_table, int fmt,
                   double* weights) {
     S2G_TRY(check_bw(bw));
-    if (!rdata || !idata || !rres || !ires || !cos_pml_table) return fail(S2G_ERR_ARG, "NULL argument");
+    if (!rdata || !idata || !rres || !ires) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(dropin_device());
     Tables* base;
     S2G_TRY(get_tables(bw, bw, &base));
@@ -373,8 +373,10 @@ static int do_fzt(double* rdata, double* idata, double* rres, double* ires, int 
     void* work = c.take(f64_work_bytes(bw, 1, REAL) / sizeof(double));
     S2G_CUDA(cudaMemcpy(dr, rdata, ng * 8, cudaMemcpyHostToDevice));
     S2G_CUDA(cudaMemcpy(di, idata, ng * 8, cudaMemcpyHostToDevice));
-    S2G_CUDA(cudaMemcpy(tab, cos_pml_table, nt * 8, cudaMemcpyHostToDevice));
-    view.fwd = tab;
+    if (cos_pml_table) {  // null: the device's own order-0 table (on the fly)
+        S2G_CUDA(cudaMemcpy(tab, cos_pml_table, nt * 8, cudaMemcpyHostToDevice));
+        view.fwd = tab;
+    }
     if (weights) {
         S2G_CUDA(cudaMemcpy(dw, weights, 4 * (size_t)bw * 8, cudaMemcpyHostToDevice));
         view.weights = dw;
@@ -612,6 +614,34 @@ void ConvOn2SphereSemiMemo(double* rdata, double* idata, double* rfilter, double
                            double* ires, const int bw, double* workspace) {
     (void)workspace;
     report("ConvOn2SphereSemiMemo", do_conv(rdata, idata, rfilter, ifilter, rres, ires, bw));
+}
+
+// On-the-fly family (src/FST_semi_fly.c): the reference generates each order's table inside the
+// call; here the tables are generated on the GPU for (bw, cutoff) on first use and kept for the
+// next call, so the transforms are those of the memo family on the device's own tables.
+void FSTSemiFly(double* rdata, double* idata, double* rcoeffs, double* icoeffs, const int bw, double* workspace,
+                DataFormat data_format, const int cutoff, fftw_plan* DCT_plan, fftw_plan* FFT_plan,
+                double* weights) {
+    (void)workspace; (void)DCT_plan; (void)FFT_plan;
+    report("FSTSemiFly", do_fst(rdata, idata, rcoeffs, icoeffs, bw, nullptr, (int)data_format, cutoff, weights));
+}
+
+void InvFSTSemiFly(double* rcoeffs, double* icoeffs, double* rdata, double* idata, const int bw, double* workspace,
+                   DataFormat data_format, const int cutoff, fftw_plan* inv_DCT_plan, fftw_plan* inv_FFT_plan) {
+    (void)workspace; (void)inv_DCT_plan; (void)inv_FFT_plan;
+    report("InvFSTSemiFly", do_inv_fst(rcoeffs, icoeffs, rdata, idata, bw, nullptr, (int)data_format, cutoff));
+}
+
+void FZTSemiFly(double* rdata, double* idata, double* rres, double* ires, const int bw, double* workspace,
+                DataFormat data_format, fftw_plan* DCT_plan, double* weights) {
+    (void)workspace; (void)DCT_plan;
+    report("FZTSemiFly", do_fzt(rdata, idata, rres, ires, bw, nullptr, (int)data_format, weights));
+}
+
+void ConvOn2SphereSemiFly(double* rdata, double* idata, double* rfilter, double* ifilter, double* rres,
+                          double* ires, const int bw, double* workspace) {
+    (void)workspace;
+    report("ConvOn2SphereSemiFly", do_conv(rdata, idata, rfilter, ifilter, rres, ires, bw));
 }
 
 void DLTSemi(double* data, const int bw, const int m, double* result, double* workspace, double* cos_pml_table,

@@ -16,7 +16,8 @@ Two kinds of fixture are written (all float64, np.savez_compressed):
     documented for them (Y_2^0, Y_3^1, (sqrt2 + pi i) Y_4^3, Y_1^1 + (3-2i) Y_5^-2).
 * outputs of the unmodified reference C sources compiled by `make -C oracle ref`
   (FSTSemiMemo, InvFSTSemiMemo, FZTSemiMemo, ConvOn2SphereSemiMemo, DLTSemi/InvDLTSemi,
-  table generators, GenerateWeightsForDLT) on seeded inputs -> ref_*.npz.
+  table generators, GenerateWeightsForDLT) on seeded inputs -> ref_*.npz, and of the
+  on-the-fly family (FSTSemiFly, InvFSTSemiFly, FZTSemiFly, ConvOn2SphereSemiFly) -> ref_fly.npz.
 """
 from __future__ import annotations
 
@@ -122,6 +123,37 @@ def main():
                             inv=inv)
     np.savez_compressed(os.path.join(out, "ref_weights.npz"), w16=r.weights(16), w64=r.weights(64),
                         w256=r.weights(256))
+
+    # on-the-fly family (FST_semi_fly.c) on seeded inputs: forward of a noisy grid, inverse of
+    # random coefficients, FZT, and the convolution of a noisy signal with a zonal filter grid
+    rng = np.random.default_rng(20261204)
+    fly = {}
+    for bw, cut, fmt in ((16, 16, REAL), (16, 6, COMPLEX), (32, 32, REAL), (32, 20, COMPLEX)):
+        tag = f"bw{bw}_cut{cut}_{'real' if fmt else 'complex'}"
+        nr = rng.standard_normal(4 * bw * bw)
+        ni = rng.standard_normal(4 * bw * bw) if fmt == COMPLEX else np.zeros(4 * bw * bw)
+        if fmt == REAL:
+            rc, ic = real_field_coeffs(rng, bw, 1.0)
+        else:
+            rc, ic = rng.standard_normal(bw * bw), rng.standard_normal(bw * bw)
+        fr_, fi_ = r.fst_fly(nr, ni, bw, fmt, cut)
+        gr_, gi_ = r.inv_fst_fly(rc, ic, bw, fmt, cut)
+        fly.update({f"{tag}_grid_r": nr, f"{tag}_grid_i": ni, f"{tag}_fst_r": fr_, f"{tag}_fst_i": fi_,
+                    f"{tag}_coef_r": rc, f"{tag}_coef_i": ic, f"{tag}_inv_r": gr_, f"{tag}_inv_i": gi_})
+    bw = 16
+    zr_, zi_ = rng.standard_normal(4 * bw * bw), rng.standard_normal(4 * bw * bw)
+    fly["fzt_bw16_data_r"], fly["fzt_bw16_data_i"] = zr_, zi_
+    fly["fzt_bw16_complex_r"], fly["fzt_bw16_complex_i"] = r.fzt_fly(zr_, zi_, bw, COMPLEX)
+    fly["fzt_bw16_real_r"], fly["fzt_bw16_real_i"] = r.fzt_fly(zr_, zi_, bw, REAL)
+    hr = np.zeros(bw * bw)
+    for l in range(bw):
+        hr[r.lib.IndexOfHarmonicCoeff(0, l, bw)] = np.exp(-l * (l + 1) / (2 * 6.0 ** 2))
+    filt_r, _ = r.inv_fst(hr, np.zeros(bw * bw), bw, REAL, bw)
+    sig = rng.standard_normal(4 * bw * bw)
+    fly["conv_bw16_signal"], fly["conv_bw16_filter"] = sig, filt_r
+    fly["conv_bw16_out_r"], fly["conv_bw16_out_i"] = r.conv_fly(sig, np.zeros(4 * bw * bw), filt_r,
+                                                                np.zeros(4 * bw * bw), bw)
+    np.savez_compressed(os.path.join(out, "ref_fly.npz"), **fly)
 
     print("fixtures written to", out)
 

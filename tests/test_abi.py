@@ -24,7 +24,8 @@ def declared_functions():
 
 def test_header_declares_expected_api():
     names = declared_functions()
-    for n in ("FSTSemiMemo", "InvFSTSemiMemo", "FZTSemiMemo", "ConvOn2SphereSemiMemo", "DLTSemi", "InvDLTSemi",
+    for n in ("FSTSemiMemo", "InvFSTSemiMemo", "FZTSemiMemo", "ConvOn2SphereSemiMemo", "FSTSemiFly", "InvFSTSemiFly",
+              "FZTSemiFly", "ConvOn2SphereSemiFly", "DLTSemi", "InvDLTSemi",
               "SemiNaive_Naive_Pml_Table", "s2g_plan_create", "s2g_fst_real_f32"):
         assert n in names
 

@@ -150,3 +150,31 @@ def test_oracle_matches_reference_build(oracle):
     for bw in (8, 17, 64):
         for m in range(bw):
             assert oracle.table_size(m, bw) == ref.lib.TableSize(m, bw)
+
+
+FLY_CASES = [(16, 16, REAL), (16, 6, COMPLEX), (32, 32, REAL), (32, 20, COMPLEX)]
+
+
+@pytest.mark.parametrize("bw,cut,fmt", FLY_CASES)
+def test_oracle_matches_reference_fly(oracle, golden, bw, cut, fmt):
+    """The on-the-fly family (FST_semi_fly.c) computes the memo family's transforms: the oracle's
+    memo restatement reproduces the reference's FSTSemiFly / InvFSTSemiFly outputs (ref_fly.npz)."""
+    g = golden("ref_fly")
+    tag = f"bw{bw}_cut{cut}_{'real' if fmt else 'complex'}"
+    a = oracle.fst(g[f"{tag}_grid_r"], g[f"{tag}_grid_i"], bw, fmt, cut)
+    assert rel_err_norm(*a, g[f"{tag}_fst_r"], g[f"{tag}_fst_i"]) <= 1e-14
+    b = oracle.inv_fst(g[f"{tag}_coef_r"], g[f"{tag}_coef_i"], bw, fmt, cut)
+    assert rel_err_norm(*b, g[f"{tag}_inv_r"], g[f"{tag}_inv_i"]) <= 1e-14
+
+
+def test_oracle_matches_reference_fly_fzt_conv(oracle, golden):
+    g = golden("ref_fly")
+    for fmt, key in ((COMPLEX, "complex"), (REAL, "real")):
+        zr, zi = oracle.fzt(g["fzt_bw16_data_r"], g["fzt_bw16_data_i"], 16, fmt)
+        assert rel_err_norm(zr, zi[:16], g[f"fzt_bw16_{key}_r"], g[f"fzt_bw16_{key}_i"][:16]) <= 1e-14
+        # REAL: the reference zeroes 2*bw imaginary values (FST_semi_fly.c:424)
+        if fmt == REAL:
+            assert not g["fzt_bw16_real_i"].any()
+    z = np.zeros(4 * 16 * 16)
+    cr, ci = oracle.conv(g["conv_bw16_signal"], z, g["conv_bw16_filter"], z, 16)
+    assert rel_err_norm(cr, ci, g["conv_bw16_out_r"], g["conv_bw16_out_i"]) <= 1e-14
