@@ -152,6 +152,18 @@ const char* s2g_version(void);
 /* Drops every cached device table and uploaded caller table (all devices). */
 int s2g_cache_clear(void);
 
+/* Table files: the device's FP64 seminaive/naive tables for (bw, cutoff) -- the forward
+ * (SemiNaive_Naive_Pml_Table, cospml.c:451-475) and transposed (cospml.c:490-518) layouts --
+ * written to `path` (generated first if needed), and read back into the current device's table
+ * cache in another process, so that plans and drop-ins for (bw, cutoff) use them without
+ * generating.  The file holds a 64-byte header (magic "S2GTAB1", bw, cutoff, doubles per table,
+ * an FNV-1a hash of the payload) and both tables; loading rejects a wrong magic, sizes that do
+ * not match bw and cutoff, a short file or a hash mismatch, and tables that already exist on
+ * the device.  No counterpart in the reference, which regenerates its tables in every
+ * process. */
+int s2g_tables_save(int bw, int cutoff, const char* path);
+int s2g_tables_load(const char* path, int* bw, int* cutoff);
+
 typedef struct s2g_plan_s* s2g_plan;
 
 /* Creates a plan for bandwidth bw (2 <= bw <= 2048 for powers of two, any bw <= 512 otherwise) and a

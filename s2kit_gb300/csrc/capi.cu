@@ -768,6 +768,107 @@ int IndexOfHarmonicCoeff(const int m, const int l, const int bw) { return index_
 const char* s2g_last_error(void) { return g_last_error.c_str(); }
 const char* s2g_version(void) { return "s2kit_gb300 0.1 (sm_103a)"; }
 
+// ---- table files: the device tables of (bw, cutoff) saved to disk and loaded back ----
+// Layout: 64-byte header {magic "S2GTAB1\0", int32 bw, int32 cutoff, int64 doubles per table,
+// uint64 FNV-1a hash of the payload, 32 reserved bytes}, then the forward table and the
+// transposed table (FP64, host byte order), exactly the device copies.
+namespace {
+struct TabFileHeader {
+    char magic[8];
+    int32_t bw, cutoff;
+    int64_t total;
+    uint64_t hash;
+    int64_t reserved[4];
+};
+static_assert(sizeof(TabFileHeader) == 64, "table file header");
+const char kTabMagic[8] = {'S', '2', 'G', 'T', 'A', 'B', '1', '\0'};
+
+uint64_t fnv1a(const void* p, size_t n, uint64_t h = 1469598103934665603ull) {
+    const unsigned char* c = (const unsigned char*)p;
+    for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    return h;
+}
+
+int64_t tables_total(int bw, int cutoff) {
+    int64_t n = 0;
+    for (int m = 0; m < bw; ++m) n += order_size(bw, cutoff, m);
+    return n;
+}
+}  // namespace
+
+int s2g_tables_save(int bw, int cutoff, const char* path) {
+    S2G_TRY(check_bw(bw));
+    S2G_TRY(check_cutoff(bw, cutoff));
+    if (!path) return fail(S2G_ERR_ARG, "NULL path");
+    S2G_TRY(dropin_device());
+    Tables* t;
+    S2G_TRY(get_tables(bw, cutoff, &t));
+    TabRef tref_{t};
+    std::vector<double> buf(2 * (size_t)t->total);
+    S2G_CUDA(cudaMemcpy(buf.data(), t->fwd, sizeof(double) * t->total, cudaMemcpyDeviceToHost));
+    S2G_CUDA(cudaMemcpy(buf.data() + t->total, t->inv, sizeof(double) * t->total, cudaMemcpyDeviceToHost));
+    TabFileHeader h{};
+    memcpy(h.magic, kTabMagic, 8);
+    h.bw = bw, h.cutoff = cutoff, h.total = t->total;
+    h.hash = fnv1a(buf.data(), sizeof(double) * buf.size());
+    FILE* fp = fopen(path, "wb");
+    if (!fp) return fail(S2G_ERR_ARG, "cannot write %s", path);
+    const bool ok = fwrite(&h, sizeof h, 1, fp) == 1 && fwrite(buf.data(), sizeof(double), buf.size(), fp) == buf.size();
+    if (fclose(fp) != 0 || !ok) return fail(S2G_ERR_ARG, "writing %s failed", path);
+    return S2G_OK;
+}
+
+int s2g_tables_load(const char* path, int* bw_out, int* cutoff_out) {
+    if (!path) return fail(S2G_ERR_ARG, "NULL path");
+    FILE* fp = fopen(path, "rb");
+    if (!fp) return fail(S2G_ERR_ARG, "cannot open %s", path);
+    TabFileHeader h{};
+    if (fread(&h, sizeof h, 1, fp) != 1 || memcmp(h.magic, kTabMagic, 8) != 0) {
+        fclose(fp);
+        return fail(S2G_ERR_ARG, "%s is not a table file", path);
+    }
+    int r = check_bw(h.bw);
+    if (r == S2G_OK) r = check_cutoff(h.bw, h.cutoff);
+    if (r == S2G_OK && h.total != tables_total(h.bw, h.cutoff))
+        r = fail(S2G_ERR_ARG, "%s: %lld doubles per table, bw %d cutoff %d needs %lld", path, (long long)h.total,
+                 h.bw, h.cutoff, (long long)tables_total(h.bw, h.cutoff));
+    if (r != S2G_OK) {
+        fclose(fp);
+        return r;
+    }
+    std::vector<double> buf(2 * (size_t)h.total);
+    const bool got = fread(buf.data(), sizeof(double), buf.size(), fp) == buf.size();
+    fclose(fp);
+    if (!got) return fail(S2G_ERR_ARG, "%s is truncated", path);
+    if (fnv1a(buf.data(), sizeof(double) * buf.size()) != h.hash)
+        return fail(S2G_ERR_ARG, "%s: payload hash mismatch (corrupt file)", path);
+    S2G_TRY(dropin_device());
+    int dev;
+    S2G_TRY(current_device(&dev));
+    {
+        std::lock_guard<std::mutex> lk(g_tab_mu);
+        const auto key = std::make_tuple(dev, (int)h.bw, (int)h.cutoff);
+        if (g_tables.count(key))
+            return fail(S2G_ERR_ARG, "tables for bw %d cutoff %d already exist on device %d (s2g_cache_clear first)",
+                        h.bw, h.cutoff, dev);
+        Tables* t = new Tables();
+        t->bw = h.bw, t->cutoff = h.cutoff, t->device = dev;
+        cudaStream_t st;
+        S2G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        r = build_tables(t, st, buf.data(), buf.data() + h.total);
+        cudaStreamDestroy(st);
+        if (r != S2G_OK) {
+            free_tables(t);
+            return r;
+        }
+        t->refs = 1;  // the cache's own reference
+        g_tables[key] = t;
+    }
+    if (bw_out) *bw_out = h.bw;
+    if (cutoff_out) *cutoff_out = h.cutoff;
+    return S2G_OK;
+}
+
 int s2g_cache_clear(void) {
     std::lock_guard<std::mutex> lk(g_tab_mu);
     for (auto& kv : g_tables)

@@ -78,7 +78,9 @@ struct TabRef {
     ~TabRef() { put_tables(t); }
 };
 // Build tables into caller-visible device buffers (used by the host table builders).
-int build_tables(Tables* t, cudaStream_t st);
+// Allocates and fills t's device tables; with h_fwd/h_inv (host copies of total doubles each,
+// e.g. read from a table file) the Legendre tables are uploaded instead of generated.
+int build_tables(Tables* t, cudaStream_t st, const double* h_fwd = nullptr, const double* h_inv = nullptr);
 int generate_weights_device(int bw, double* d_weights, cudaStream_t st);
 int generate_cos_pml_device(int bw, int m_begin, int m_end, double* d_fwd, const int64_t* d_off,
                             cudaStream_t st);

@@ -320,7 +320,7 @@ static void host_offsets(int bw, int cutoff, std::vector<int64_t>& off, int64_t*
     *total = o;
 }
 
-int build_tables(Tables* t, cudaStream_t st) {
+int build_tables(Tables* t, cudaStream_t st, const double* h_fwd, const double* h_inv) {
     const int B = t->bw, S = 2 * B;
     std::vector<int64_t> off;
     host_offsets(B, t->cutoff, off, &t->total);
@@ -338,6 +338,12 @@ int build_tables(Tables* t, cudaStream_t st) {
     S2G_TRY(nodes_device(S, t->sinv, 2, st));
     S2G_TRY(twiddles_device(S, t->tw_S, t->tw_D, st));
     const int cut = t->cutoff;
+    if (h_fwd && h_inv) {
+        S2G_CUDA(cudaMemcpyAsync(t->fwd, h_fwd, sizeof(double) * (size_t)t->total, cudaMemcpyHostToDevice, st));
+        S2G_CUDA(cudaMemcpyAsync(t->inv, h_inv, sizeof(double) * (size_t)t->total, cudaMemcpyHostToDevice, st));
+        S2G_CUDA(cudaStreamSynchronize(st));
+        return S2G_OK;
+    }
     S2G_TRY(generate_cos_pml_device(B, 0, cut, t->fwd, t->off, st));
     S2G_TRY(transpose_cos_pml_device(B, 0, cut, t->fwd, t->inv, t->off, st));
     if (cut < B) {
