@@ -170,8 +170,7 @@ def algorithmic_bytes(kernel, B, N):
         "dct_fwd_f32": 2 * N * ns * S * f + 2 * N * ns * B * f,
         "leg_tc_fwd": 2 * N * ns * B * f + 2 * N * nn * S * f + 2 * N * B * B * f,
         "leg_tc_inv": 2 * N * (B * (B + 1) // 2) * f + 2 * N * ns * B * f + 2 * N * nn * S * f,
-        "dct_inv_f32": 2 * N * ns * B * f + 2 * N * ns * S * f,
-        "naive_combine_f32": 2 * 2 * N * nn * S * f,
+        "dct_inv_f32": 2 * N * ns * B * f + 2 * N * ns * S * f + 2 * 2 * N * nn * S * f,
         "rows_inv_f32": 2 * N * B * S * f + N * S * S * f,
     }
     return table.get(kernel)

@@ -5,14 +5,14 @@
 //   k_rows_fwd_w       : DFT along phi (warp FFT, two real latitudes per warp), X[p][f][m][theta]
 //   k_dct_fwd_w        : weights (even/odd order) + REDFT10 + normalisation (seminaive.c:161-176)
 //                        -> C[p][f][m][t][j], cosine frequency k = 2j + t (parity-split)
-//   k_leg_fwd_tc       : per (order m, 64 functions): for each parity t of (l - m), the dense
+//   k_leg_ws (forward) : per (order m, 64 functions): for each parity t of (l - m), the dense
 //                        trapezoid T_{m,t}[i][j] = T(m, l = m+t+2i, k = 2j+t) times C (seminaive.c:183-197)
 //                        as D[128 x N] = A[128 x K] * B[N x K]^T on tcgen05, A = 64 functions x
 //                        (re, im) rows, B = table rows; epilogue writes f(l, m) and f(l, -m).
 // Inverse (InvFSTSemiMemo, REAL; FST_semi_memo.c:228-351):
-//   k_leg_inv_tc       : fcos[2j+t] = sum_i T_{m,t}[i][j] a(m + t + 2i) (seminaive.c:74-98), scaled
-//   k_dct_inv_w        : REDFT01, sin(theta) for odd m, 1/sqrt(2 pi)
-//   k_naive_combine    : naive orders (odd m < 32): even/odd latitude halves back to samples
+//   k_leg_ws (inverse) : fcos[2j+t] = sum_i T_{m,t}[i][j] a(m + t + 2i) (seminaive.c:74-98), scaled
+//   k_dct_inv_w        : REDFT01, sin(theta) for odd m, 1/sqrt(2 pi); naive orders (odd m < 32):
+//                        even/odd latitude halves back to samples
 //   k_rows_inv_w       : DFT with sign +1 over m, Hermitian rows, two latitudes per warp
 //
 // Precision: x = x0 + x1 + x2 with BF16 terms (each the rounded residual of the previous);
@@ -448,10 +448,13 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
     float* spi = spr + W * PSA;        // [W][PSA] im
     float2* tw = reinterpret_cast<float2*>(spi + W * PSA);
     float2* twb = tw + twtab_len(S);
-    const int f = blockIdx.y, th0 = blockIdx.x * LAT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     load_tw(tw, twb, nullptr, gtw, nullptr, S);
     __syncthreads();
+    // CTA-strided (function, latitude block) tiles; launched with one tile per CTA
+    constexpr int NLB = S / LAT;
+    for (int tile = blockIdx.x; tile < N * NLB; tile += gridDim.x) {
+    const int f = tile / NLB, th0 = (tile - f * NLB) * LAT;
     float2 v[R];
     {
         const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + 2 * warp) * S;
@@ -489,6 +492,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
         *reinterpret_cast<float4*>(X + o) = make_float4(re[0], re[1], re[2], re[3]);
         *reinterpret_cast<float4*>(X + plane + o) = make_float4(im[0], im[1], im[2], im[3]);
     }
+    __syncthreads();  // every warp's spectrum has been read before the next tile overwrites it
+    }
 }
 
 // Weighted REDFT10 per (function, seminaive order) row, stored by parity of the cosine index:
@@ -518,8 +523,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
     for (int q = threadIdx.x; q < 2 * S; q += blockDim.x) w[q] = gw[q];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * W + warp;
-    if (row >= nrows) return;
+    // persistent: the tables are loaded once, then each warp walks rows
+    for (int row = blockIdx.x * W + warp; row < nrows; row += gridDim.x * W) {
     const int m = row % B;
     float* xr = X + (size_t)row * S;
     float* xi = xr + (size_t)nrows * S;
@@ -544,7 +549,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
             reinterpret_cast<float4*>(xi)[e] = make_float4(c[0], c[1], c[2], c[3]);
             reinterpret_cast<float4*>(xi + B)[e] = make_float4(d[0], d[1], d[2], d[3]);
         }
-        return;
+        __syncwarp();  // the staged row is read before the next row overwrites it
+        continue;
     }
     const float* ws = w + ((m & 1) ? S : 0);
     float2 v[R];
@@ -587,6 +593,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
         reinterpret_cast<float4*>(cr)[e] = make_float4(a[0], a[1], a[2], a[3]);
         reinterpret_cast<float4*>(ci)[e] = make_float4(b[0], b[1], b[2], b[3]);
     }
+    __syncwarp();  // the spectrum is read before the next row's transform overwrites it
+    }
 }
 
 // REDFT01 per (function, seminaive order) row, sin(theta) for odd m, scale: F[p][f][m][theta].
@@ -609,12 +617,39 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     for (int q = threadIdx.x; q < S; q += blockDim.x) sn[q] = gsin[q];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * W + warp;
-    if (row >= nrows) return;
-    const int m = row % B;
-    if (naive_order(m)) return;
     float* zr = spr + warp * PSA;
     float* zi = spi + warp * PSA;
+    // persistent: the tables are loaded once, then each warp walks rows
+    for (int row = blockIdx.x * W + warp; row < nrows; row += gridDim.x * W) {
+    const int m = row % B;
+    if (naive_order(m)) {
+        // Naive orders: the contraction left D0 (even l - m) in F[..][0, B) and D1 (odd l - m) in
+        // F[..][B, 2B) for the northern latitudes; P(m,l)(-x) = (-1)^(l-m) P(m,l)(x) gives
+        // F[theta] = D0 + D1 and F[2B-1-theta] = D0 - D1 (times 1/sqrt(2 pi)), in place.
+        float* fr = F + (size_t)row * S;
+        float* fi = fr + (size_t)nrows * S;
+        for (int e = lane; e < S / 4; e += 32) {
+            reinterpret_cast<float4*>(zr)[e] = reinterpret_cast<const float4*>(fr)[e];
+            reinterpret_cast<float4*>(zi)[e] = reinterpret_cast<const float4*>(fi)[e];
+        }
+        __syncwarp();
+        for (int e = lane; e < B / 4; e += 32) {
+            float lo[4], hi[4], lo2[4], hi2[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float d0 = zr[4 * e + u], d1 = zr[B + 4 * e + u], c0 = zi[4 * e + u], c1 = zi[B + 4 * e + u];
+                lo[u] = (d0 + d1) * scale, hi[u] = (d0 - d1) * scale;
+                lo2[u] = (c0 + c1) * scale, hi2[u] = (c0 - c1) * scale;
+            }
+            reinterpret_cast<float4*>(fr)[e] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+            reinterpret_cast<float4*>(fi)[e] = make_float4(lo2[0], lo2[1], lo2[2], lo2[3]);
+            // F[S-1-(4e+u)] for u = 3..0 is the aligned run starting at S-4-4e
+            reinterpret_cast<float4*>(fr + S - 4 - 4 * e)[0] = make_float4(hi[3], hi[2], hi[1], hi[0]);
+            reinterpret_cast<float4*>(fi + S - 4 - 4 * e)[0] = make_float4(hi2[3], hi2[2], hi2[1], hi2[0]);
+        }
+        __syncwarp();
+        continue;
+    }
     // Fc[p][f][m][t][j]: cosine coefficient k = 2j + t at (k & 1) * B/2 + k/2
     const float* xa = Fc + (size_t)row * B;
     const float* xb = Fc + (size_t)(nrows + row) * B;
@@ -656,6 +691,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
         reinterpret_cast<float4*>(fr)[e] = make_float4(a[0], a[1], a[2], a[3]);
         reinterpret_cast<float4*>(fi)[e] = make_float4(b[0], b[1], b[2], b[3]);
     }
+    __syncwarp();  // the spectrum is read before the next row's transform overwrites it
+    }
 }
 
 // DFT with sign +1 over the orders for LAT latitudes (two real output rows per warp).  The
@@ -678,10 +715,13 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
     float* spi = spr + W * PSA;
     float2* tw = reinterpret_cast<float2*>(fsm + U);
     float2* twb = tw + twtab_len(S);
-    const int f = blockIdx.y, th0 = blockIdx.x * LAT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     load_tw(tw, twb, nullptr, gtw, nullptr, S);
     const size_t plane = (size_t)N * B * S;
+    // CTA-strided (function, latitude block) tiles; launched with one tile per CTA
+    constexpr int NLB = S / LAT;
+    for (int tile = blockIdx.x; tile < N * NLB; tile += gridDim.x) {
+    const int f = tile / NLB, th0 = (tile - f * NLB) * LAT;
     constexpr int Q4 = LAT / 4;
     // loads of up to four iterations are issued before their shared-memory stores
     constexpr int NIT = (B * Q4 + T - 1) / T, BAT = NIT < 4 ? NIT : 4;
@@ -749,24 +789,7 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
         reinterpret_cast<float4*>(ga + S)[e] =
             make_float4(zi[pad32(k)], zi[pad32(k + 1)], zi[pad32(k + 2)], zi[pad32(k + 3)]);
     }
-}
-
-// Naive inverse orders: the contraction left D0 (even l-m) in F[..][0, B) and D1 (odd l-m)
-// in F[..][B, 2B) for the northern latitudes; P(m,l)(-x) = (-1)^(l-m) P(m,l)(x) gives
-// F[theta] = D0 + D1 and F[2B-1-theta] = D0 - D1 (times 1/sqrt(2 pi)).
-__global__ void k_naive_combine(float* F, int N, int B, float scale) {
-    extern __shared__ __align__(16) float fsm[];
-    const int S = 2 * B;
-    const int nnaive = (B < kNaiveOddBelow ? B : kNaiveOddBelow) / 2;
-    const int f = blockIdx.x / nnaive, m = 2 * (blockIdx.x % nnaive) + 1;
-    const int part = blockIdx.y;
-    float* row = F + (((size_t)part * N + f) * B + m) * S;
-    for (int q = threadIdx.x; q < S; q += blockDim.x) fsm[q] = row[q];
-    __syncthreads();
-    for (int th = threadIdx.x; th < B; th += blockDim.x) {
-        const float d0 = fsm[th], d1 = fsm[B + th];
-        row[th] = (d0 + d1) * scale;
-        row[S - 1 - th] = (d0 - d1) * scale;
+    __syncthreads();  // the spectra (aliasing the tile) are read before the next tile is loaded
     }
 }
 
@@ -2072,6 +2095,30 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     return S2G_OK;
 }
 
+// Grid of a persistent kernel: the CTAs that fit on the GPU at once (cached per kernel and
+// shared-memory size), at most `blocks`.
+static int persistent_grid(const void* fn, int threads, size_t smem, long long blocks, int* grid) {
+    static std::mutex mu;
+    static std::vector<std::pair<std::pair<const void*, size_t>, int>> cache;
+    int per_gpu = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto& e : cache)
+            if (e.first.first == fn && e.first.second == smem) per_gpu = e.second;
+    }
+    if (!per_gpu) {
+        int occ = 0, dev = 0, nsm = 0;
+        S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem));
+        S2G_CUDA(cudaGetDevice(&dev));
+        S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        per_gpu = std::max(1, occ) * nsm;
+        std::lock_guard<std::mutex> lk(mu);
+        cache.push_back({{fn, smem}, per_gpu});
+    }
+    *grid = (int)std::max<long long>(1, std::min<long long>(blocks, per_gpu));
+    return S2G_OK;
+}
+
 // ---- warp-FFT kernel launchers (dispatch on R = S / 32) ----
 template <int R>
 static int launch_fft_kernels(int which, const void* in, void* out, int N, const Split* s, cudaStream_t st,
@@ -2085,25 +2132,29 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
     if (which == 0) {  // rows forward
         smem = spec + tw_bytes;
         S2G_TRY(set_smem((const void*)k_rows_fwd_w<R>, smem));
-        dim3 g(S / kLatPerCta, N);
+        const int g = N * (S / kLatPerCta);  // one tile per CTA: fresh CTAs overlap loads better than a loop
         ProfScope ps_("rows_fwd_f32", st);
         k_rows_fwd_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, N, scale, s->twS, gmap);
     } else if (which == 1) {  // DCT-II
         smem = spec + sizeof(float) * 2 * S + sizeof(float2) * B + tw_bytes;
         S2G_TRY(set_smem((const void*)k_dct_fwd_w<R>, smem));
+        int g;
+        S2G_TRY(persistent_grid((const void*)k_dct_fwd_w<R>, kThreads, smem, (nrows + kWarps - 1) / kWarps, &g));
         ProfScope ps_("dct_fwd_f32", st);
-        k_dct_fwd_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((float*)in, (float*)out, nrows, s->w32,
+        k_dct_fwd_w<R><<<g, kThreads, smem, st>>>((float*)in, (float*)out, nrows, s->w32,
                                                                         s->twS, s->twD);
     } else if (which == 2) {  // DCT-III
         smem = spec + sizeof(float) * S + sizeof(float2) * S + tw_bytes;
         S2G_TRY(set_smem((const void*)k_dct_inv_w<R>, smem));
+        int g;
+        S2G_TRY(persistent_grid((const void*)k_dct_inv_w<R>, kThreads, smem, (nrows + kWarps - 1) / kWarps, &g));
         ProfScope ps_("dct_inv_f32", st);
-        k_dct_inv_w<R><<<(nrows + kWarps - 1) / kWarps, kThreads, smem, st>>>((const float*)in, (float*)out, nrows,
+        k_dct_inv_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, nrows,
                                                                         s->sin32, s->twS, s->twD, scale);
     } else {  // rows inverse
         smem = std::max(sizeof(float) * 2 * B * L::TS, spec) + tw_bytes;
         S2G_TRY(set_smem((const void*)k_rows_inv_w<R>, smem));
-        dim3 g(S / kLatPerCta, N);
+        const int g = N * (S / kLatPerCta);  // one tile per CTA: fresh CTAs overlap loads better than a loop
         ProfScope ps_("rows_inv_f32", st);
         k_rows_inv_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, N, s->twS, gmap);
     }
@@ -2180,16 +2231,11 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
 int split_inv_tail(Tables* t, float* F, float* Fc, float* grid, int batch, const int64_t* gmap, cudaStream_t st) {
     S2G_TRY(build_split(t));
     Split* s = (Split*)t->split;
-    const int B = t->bw, S = 2 * B;
+    const int B = t->bw;
     const float scale = (float)(1.0 / sqrt(2.0 * kPi));
-    // REDFT01 (+ sin(theta) for odd m), scaled by 1/sqrt(2 pi)              (seminaive.c:105-114)
+    // REDFT01 (+ sin(theta) for odd m), scaled by 1/sqrt(2 pi), and the naive orders' even/odd
+    // latitude halves recombined                                             (seminaive.c:105-114)
     S2G_TRY(fft_kernels(2, B, Fc, F, batch, s, st, scale));
-    {
-        const int nnaive = std::min(B, kNaiveOddBelow) / 2;
-        ProfScope ps_("naive_combine_f32", st);
-        k_naive_combine<<<dim3(batch * nnaive, 2), 256, S * sizeof(float), st>>>(F, batch, B, scale);
-        S2G_CUDA(cudaGetLastError());
-    }
     // DFT with sign +1 over the orders, Hermitian rows                      (FST_semi_memo.c:334-350)
     return fft_kernels(3, B, F, grid, batch, s, st, 1.f, gmap);
 }
