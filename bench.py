@@ -389,6 +389,9 @@ def main():
     d2h = h_grid.nbytes + h_orc.nbytes + h_oic.nbytes
     # ---- grouped uneven-bandwidth workload (one graph per step), reported beside the headline
     grp = group_bench(api, torch, stream, args.steps, args.warmup, args.seed) if args.group else None
+    # ---- BASELINE configs 3 and 5, timed beside the headline
+    cfg3 = config3_bench(api, torch, stream, args.seed) if args.group else None
+    cfg5 = config5_bench(api, torch, stream, args.seed) if args.group else None
     clk = clocks.stop()
 
     # ---- CPU baseline (rank 0): bounded sample of the same workload on all host cores
@@ -422,10 +425,94 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
             "group": grp,
+            "config3": cfg3,
+            "config5": cfg5,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _time(torch, stream, fn, reps):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def config3_bench(api, torch, stream, seed):
+    """BASELINE config 3: 4096 real functions at bw 64, FP32 grids, coefficients N(0,1)(1+l)^-1.5,
+    split BF16X3 fwd+inv; error of the split forward against the FP64 path on the same grid."""
+    B, N = 64, 4096
+    rc, ic = real_field_coeffs(np.random.default_rng(seed + 3), B, 1.5, N)
+    plan = api.Plan(B, B)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    g64 = torch.empty(N, 4 * B * B, dtype=torch.float64, device="cuda")
+    plan.inv_fst(d_rc, d_ic, g64, None, N, api.REAL, stream)
+    f_r, f_i = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    plan.fst(g64, None, f_r, f_i, N, api.REAL, stream)
+    g32 = g64.float()
+    s_r = torch.empty(N, B * B, dtype=torch.float32, device="cuda")
+    s_i = torch.empty_like(s_r)
+    c_r, c_i = d_rc.float(), d_ic.float()
+
+    def step():
+        plan.inv_fst_real_f32(c_r, c_i, g32, N, api.PREC_BF16X3, stream)
+        plan.fst_real_f32(g32, s_r, s_i, N, api.PREC_BF16X3, stream)
+
+    ms = _time(torch, stream, step, 20)
+    g32.copy_(g64.float())
+    plan.fst_real_f32(g32, s_r, s_i, N, api.PREC_BF16X3, stream)
+    torch.cuda.synchronize()
+    plan.sync_status()
+    mag = torch.hypot(f_r, f_i).amax(dim=1)
+    err = (torch.hypot(s_r.double() - f_r, s_i.double() - f_i).amax(dim=1) / mag).max().item()
+    return {"workload": "4096 real functions at bw 64, (1+l)^-1.5, split BF16X3, fwd+inv", "value": N / (ms / 1e3),
+            "unit": "fwd+inv functions/s", "ms_per_step": ms, "coeff_err_vs_fp64": err}
+
+
+def config5_bench(api, torch, stream, seed):
+    """BASELINE config 5: 16 real functions at bw 1024, (1+l)^-1: split BF16X3 fwd+inv, the FP64-residual
+    refined forward and the FP64 fwd+inv, with the errors against the FP64 path."""
+    B, N = 1024, 16
+    rc, ic = real_field_coeffs(np.random.default_rng(seed + 5), B, 1.0, N)
+    plan = api.Plan(B, B)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    g64 = torch.empty(N, 4 * B * B, dtype=torch.float64, device="cuda")
+    f_r, f_i = torch.empty_like(d_rc), torch.empty_like(d_ic)
+
+    def step64():
+        plan.inv_fst(d_rc, d_ic, g64, None, N, api.REAL, stream)
+        plan.fst(g64, None, f_r, f_i, N, api.REAL, stream)
+
+    ms64 = _time(torch, stream, step64, 3)
+    g32 = g64.float()
+    c_r, c_i = d_rc.float(), d_ic.float()
+    s_r = torch.empty(N, B * B, dtype=torch.float32, device="cuda")
+    s_i = torch.empty_like(s_r)
+    g32b = torch.empty_like(g32)
+
+    def step32():
+        plan.inv_fst_real_f32(c_r, c_i, g32b, N, api.PREC_BF16X3, stream)
+        plan.fst_real_f32(g32, s_r, s_i, N, api.PREC_BF16X3, stream)
+
+    ms32 = _time(torch, stream, step32, 5)
+    r_r, r_i = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    msr = _time(torch, stream, lambda: plan.fst_refined(g64, r_r, r_i, N, api.PREC_BF16X3, stream), 3)
+    plan.fst_real_f32(g32, s_r, s_i, N, api.PREC_BF16X3, stream)
+    torch.cuda.synchronize()
+    plan.sync_status()
+    mag = torch.hypot(f_r, f_i).amax(dim=1)
+    e_split = (torch.hypot(s_r.double() - f_r, s_i.double() - f_i).amax(dim=1) / mag).max().item()
+    e_ref = (torch.hypot(r_r - f_r, r_i - f_i).amax(dim=1) / mag).max().item()
+    return {"workload": "16 real functions at bw 1024, (1+l)^-1", "split_bf16x3_fwd_inv_per_s": N / (ms32 / 1e3),
+            "fp64_fwd_inv_per_s": N / (ms64 / 1e3), "refined_fwd_per_s": N / (msr / 1e3),
+            "split_fwd_err_vs_fp64": e_split, "refined_fwd_err_vs_fp64": e_ref}
 
 
 def group_bench(api, torch, stream, steps, warmup, seed):

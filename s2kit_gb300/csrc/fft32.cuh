@@ -175,29 +175,67 @@ struct WarpFFT {
     }
 };
 
-// Four-step form of the same transform for R in {16, 32}: stages (a) and (b) as above, then the
-// 32-point DFTs across the lanes go through shared memory instead of shuffles.
+// Four-step form of the same transform for R in {8, 16, 32}: stages (a) and (b) as above, then the
+// 32-point DFTs across the lanes go through shared memory instead of lane butterflies.
 //   (c1) lane l writes u_l[k1] to row k1, column l of the warp's exchange planes (row stride
-//        32 + P floats, P = 32 / R);
+//        32 + P floats, P = 32 / R: conflict-free in both directions);
 //   (c2) lane L = P c + h reads column c at lanes P j + h (j < R): y_j = u_{P j + h}[c], and
 //        takes their R-point DFT in registers, Y_h[k] = sum_j y_j w_R^(j k);
-//   (c3) Z_c[k + R q] = sum_h w_32^(h k) Y_h[k] w_P^(h q): nothing more for P = 1; for P = 2 the
-//        two lanes of a column swap half of their values once (lane h keeps k = 2 i + h) and
-//        finish with one butterfly.
-// Then X[c + R k2] = Z_c[k2].  Shared-memory traffic per transform: R exchange writes and reads
-// per plane (conflict-free: row stride 32 + P) and R shuffles, against 10 R shuffles of the
-// lane-butterfly form.  Register s of lane L holds X[out_index(s)]; for a fixed s the 32 lanes
-// hold 32 consecutive indices.
+//   (c3) Z_c[k + R q] = sum_h T_h[k] w_P^(h q) with T_h[k] = w_32^(h k) Y_h[k]: a P-point DFT
+//        across the P lanes of column c, as log2(P) decimation-in-frequency stages.  In stage s
+//        the partner lanes (h differing in bit e = log2(P) - 1 - s) split the k values they
+//        hold by bit e of k (each keeps those whose bit e equals its own bit e of h), swap the
+//        other half once (R shuffles per stage) and finish the butterfly, the difference twiddled
+//        by w_M^(h mod 2^e), M = P >> s.  At the end lane (c, h) holds k = P k_hi + h, k_hi < R/P,
+//        for every q.
+// Then X[c + R k2] = Z_c[k2].  Register s of lane L holds X[out_index(s)], and for a fixed s the
+// 32 lanes hold 32 consecutive indices, so spectrum stores through pad32 are conflict-free.
+// Shared-memory traffic per transform: R exchange writes and reads per plane and log2(P) R
+// shuffles, against 10 R shuffles of the lane-butterfly form.
 template <int R>
 struct WarpFFT4 {
-    static_assert(R == 16 || R == 32, "four-step warp FFT: R = 16 or 32");
+    static_assert(R == 8 || R == 16 || R == 32, "four-step warp FFT: R = 8, 16 or 32");
     static constexpr int P = 32 / R;
-    static constexpr int XS = 32 + P;   // exchange row stride (floats)
-    static constexpr int kExchangeFloats = R * XS;  // per plane
+    static constexpr int LP = P == 1 ? 0 : P == 2 ? 1 : 2;  // log2 P
+    static constexpr int XS = 32 + P;                       // exchange row stride (floats)
+    static constexpr int kExchangeFloats = R * XS;          // per plane
+
+    template <int STG>
+    __device__ __forceinline__ static void stage(float2 (&u)[R], const float2* __restrict__ tw, int h, float sign) {
+        constexpr int e = LP - 1 - STG;       // bit of h (and of k) this stage splits
+        constexpr int ncur = R >> STG;        // k values per q-combination before the stage
+        constexpr int nf = 1 << (LP - STG);   // free low bits of k, as a count
+        constexpr int hf = nf / 2;
+        constexpr int nq = 1 << STG;          // q-bit combinations so far
+        constexpr int nnew = ncur / 2;
+        constexpr int M = P >> STG;           // size of the sub-DFTs over h
+        const int b = (h >> e) & 1;
+        float2 w = tw[padtw((h & ((1 << e) - 1)) * (32 * R / M))];  // w_M^(h mod 2^e)
+        w.y *= sign;
+        float2 nv[R];
+#pragma unroll
+        for (int qb = 0; qb < nq; ++qb)
+#pragma unroll
+            for (int kh = 0; kh < R / P; ++kh)
+#pragma unroll
+                for (int f = 0; f < hf; ++f) {
+                    const int i0 = qb * ncur + kh * nf + f, i1 = i0 + hf;  // k bit e = 0 / 1
+                    const float2 own = b ? u[i1] : u[i0];
+                    const float2 snd = b ? u[i0] : u[i1];
+                    float2 rcv;
+                    rcv.x = __shfl_xor_sync(0xffffffffu, snd.x, 1 << e);
+                    rcv.y = __shfl_xor_sync(0xffffffffu, snd.y, 1 << e);
+                    const float2 lo = b ? rcv : own, hi = b ? own : rcv;
+                    const int kk = kh * hf + f;
+                    nv[qb * nnew + kk] = make_float2(lo.x + hi.x, lo.y + hi.y);
+                    nv[(qb + nq) * nnew + kk] = cmulf(make_float2(lo.x - hi.x, lo.y - hi.y), w);
+                }
+#pragma unroll
+        for (int i = 0; i < R; ++i) u[i] = nv[i];
+    }
 
     __device__ static void run(float2 (&v)[R], const float2* __restrict__ tw, const float2* __restrict__ twb,
                                float* __restrict__ xr, float* __restrict__ xi, float sign) {
-        (void)tw;
         const int lane = threadIdx.x & 31;
         // (a) in-register DIT over i
         float2 u[R];
@@ -226,37 +264,29 @@ struct WarpFFT4 {
             u[WarpFFT<R>::brev(j)] = make_float2(xr[c * XS + P * j + h], xi[c * XS + P * j + h]);
         __syncwarp();  // the exchange planes are free again (callers reuse them)
         RegStages<R, 2>::run(u, sign);
-        if (P == 1) {
+        if (P > 1) {
+            // (c3) T_h[k] = w_32^(h k) Y_h[k], then the P-point DFT across the column's lanes
+            if (h) {
 #pragma unroll
-            for (int k = 0; k < R; ++k) v[k] = u[k];
-            return;
-        }
-        // (c3), P = 2: T_1[k] = w_32^k Y_1[k]; lane h keeps k = 2 i + h and gets T_{1-h}[k] from its partner
-        if (h) {
-#pragma unroll
-            for (int k = 1; k < R; ++k) {
-                const float2 w = make_float2(ct::cosf_(k, 32), sign * ct::sinf_(k, 32));
-                u[k] = cmulf(u[k], w);
+                for (int k = 1; k < R; ++k) {
+                    float2 w = tw[padtw(((h * k) & 31) * R)];
+                    w.y *= sign;
+                    u[k] = cmulf(u[k], w);
+                }
             }
+            if (LP >= 1) stage<0>(u, tw, h, sign);
+            if (LP >= 2) stage<LP >= 2 ? 1 : 0>(u, tw, h, sign);
         }
 #pragma unroll
-        for (int i = 0; i < R / 2; ++i) {
-            const float2 own = h ? u[2 * i + 1] : u[2 * i];
-            const float2 snd = h ? u[2 * i] : u[2 * i + 1];
-            float2 rcv;
-            rcv.x = __shfl_xor_sync(0xffffffffu, snd.x, 1);
-            rcv.y = __shfl_xor_sync(0xffffffffu, snd.y, 1);
-            const float2 lo = h ? rcv : own, hi = h ? own : rcv;
-            v[i] = make_float2(lo.x + hi.x, lo.y + hi.y);
-            v[i + R / 2] = make_float2(lo.x - hi.x, lo.y - hi.y);
-        }
+        for (int k = 0; k < R; ++k) v[k] = u[k];
     }
 
+    // natural-order index of register s of this lane after run()
     __device__ __forceinline__ static int out_index(int s) {
         const int lane = threadIdx.x & 31;
-        if (P == 1) return lane + R * s;
-        const int c = lane >> 1, h = lane & 1;
-        return c + R * (2 * (s & (R / 2 - 1)) + h + 16 * (s / (R / 2)));
+        const int c = lane / P, h = lane % P;
+        const int qb = s / (R / P), kh = s % (R / P);
+        return c + R * (P * kh + h + R * qb);
     }
 };
 
@@ -272,6 +302,8 @@ struct WarpFFTSel {
     }
     __device__ __forceinline__ static int out_index(int s) { return WarpFFT<R>::out_index(s); }
 };
+template <>
+struct WarpFFTSel<8> : WarpFFT4<8> {};
 template <>
 struct WarpFFTSel<16> : WarpFFT4<16> {};
 template <>

@@ -428,7 +428,7 @@ struct FftSmem {
     static constexpr int TILE = (FftShape<R>::LAT * RS + 3) & ~3; // one plane of the row kernels' tile
     static constexpr int TS = FftShape<R>::LAT + 1;              // rows-inverse tile row (odd)
     // the four-step warp FFT exchanges through the warp's spectrum rows
-    static_assert((R != 16 && R != 32) || R * (32 + 32 / R) <= PSA, "exchange planes fit the spectrum rows");
+    static_assert((R != 8 && R != 16 && R != 32) || R * (32 + 32 / R) <= PSA, "exchange planes fit the spectrum rows");
 };
 
 // DFT along phi of LAT latitudes (two real rows per warp), transposed to X[p][f][m][theta], m < B.
