@@ -392,6 +392,7 @@ def main():
     # ---- BASELINE configs 3 and 5, timed beside the headline
     cfg3 = config3_bench(api, torch, stream, args.seed) if args.group else None
     cfg5 = config5_bench(api, torch, stream, args.seed) if args.group else None
+    cplx = complex_bench(api, torch, stream, args.seed) if args.group else None
     clk = clocks.stop()
 
     # ---- CPU baseline (rank 0): bounded sample of the same workload on all host cores
@@ -427,6 +428,7 @@ def main():
             "group": grp,
             "config3": cfg3,
             "config5": cfg5,
+            "complex": cplx,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -473,6 +475,40 @@ def config3_bench(api, torch, stream, seed):
     mag = torch.hypot(f_r, f_i).amax(dim=1)
     err = (torch.hypot(s_r.double() - f_r, s_i.double() - f_i).amax(dim=1) / mag).max().item()
     return {"workload": "4096 real functions at bw 64, (1+l)^-1.5, split BF16X3, fwd+inv", "value": N / (ms / 1e3),
+            "unit": "fwd+inv functions/s", "ms_per_step": ms, "coeff_err_vs_fp64": err}
+
+
+def complex_bench(api, torch, stream, seed):
+    """COMPLEX data at the headline size: 256 complex functions at bw 256, independent coefficients
+    N(0,1)(1+l)^-1 for every order, split BF16X3 fwd+inv; error against the FP64 COMPLEX path."""
+    B, N = 256, 256
+    rng = np.random.default_rng(seed + 7)
+    l = np.concatenate([np.arange(m, B) for m in range(B)] + [np.arange(a, B) for a in range(B - 1, 0, -1)])
+    s = (1.0 + l) ** -1.0  # degree of every slot: orders 0 .. B-1, then -(B-1) .. -1
+    d_rc = torch.from_numpy(rng.standard_normal((N, B * B)) * s).cuda()
+    d_ic = torch.from_numpy(rng.standard_normal((N, B * B)) * s).cuda()
+    plan = api.Plan(B, B)
+    g64r = torch.empty(N, 4 * B * B, dtype=torch.float64, device="cuda")
+    g64i = torch.empty_like(g64r)
+    plan.inv_fst(d_rc, d_ic, g64r, g64i, N, api.COMPLEX, stream)
+    gr, gi = g64r.float(), g64i.float()
+    del g64r, g64i
+    s_r = torch.empty(N, B * B, dtype=torch.float32, device="cuda")
+    s_i = torch.empty_like(s_r)
+    c_r, c_i = d_rc.float(), d_ic.float()
+    w_r, w_i = torch.empty_like(gr), torch.empty_like(gi)
+
+    def step():
+        plan.inv_fst_complex_f32(c_r, c_i, w_r, w_i, N, api.PREC_BF16X3, stream)
+        plan.fst_complex_f32(w_r, w_i, s_r, s_i, N, api.PREC_BF16X3, stream)
+
+    ms = _time(torch, stream, step, 20)
+    plan.fst_complex_f32(gr, gi, s_r, s_i, N, api.PREC_BF16X3, stream)
+    torch.cuda.synchronize()
+    plan.sync_status()
+    mag = torch.hypot(d_rc, d_ic).amax(dim=1)
+    err = (torch.hypot(s_r.double() - d_rc, s_i.double() - d_ic).amax(dim=1) / mag).max().item()
+    return {"workload": "256 complex functions at bw 256, (1+l)^-1, split BF16X3, fwd+inv", "value": N / (ms / 1e3),
             "unit": "fwd+inv functions/s", "ms_per_step": ms, "coeff_err_vs_fp64": err}
 
 

@@ -207,6 +207,17 @@ int s2g_fst_real_f32(s2g_plan plan, const float* grid, float* rcoeffs, float* ic
 int s2g_inv_fst_real_f32(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid, int batch,
                          int precision, void* stream);
 
+/* COMPLEX data (FSTSemiMemo / InvFSTSemiMemo with DataFormat COMPLEX, FST_semi_memo.c:146-200 and
+ * :290-333) on the split path: rgrid/igrid are the real and imaginary samples, batch*(2bw)^2
+ * floats each; rcoeffs/icoeffs batch*bw*bw floats with every order in the reference layout (the
+ * inverse reads all of them).  The field is taken as two real fields, f = g + i h, each through the
+ * real-field transforms above (same precisions, bandwidths and cutoff rule), and combined per
+ * coefficient: f(l, m) = g(l, m) + i h(l, m).  The plan holds 16*batch*bw^2 bytes of extra scratch. */
+int s2g_fst_complex_f32(s2g_plan plan, const float* rgrid, const float* igrid, float* rcoeffs, float* icoeffs,
+                        int batch, int precision, void* stream);
+int s2g_inv_fst_complex_f32(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* rgrid, float* igrid,
+                            int batch, int precision, void* stream);
+
 /* Real-field transforms with FP64 samples and coefficients whose Legendre contraction runs as
  * split products (precision: S2G_PREC_BF16X3, _BF16X2 or _FP16X2) followed by one refinement
  * step with an FP64 residual: forward a1 = F(f), a = a1 + F(f - I64(a1)); inverse g1 = I(a),

@@ -240,6 +240,16 @@ class Plan:
         check(self.lib.s2g_inv_fst_real_f32(self.h, _addr(rcoeffs), _addr(icoeffs), _addr(grid), batch, precision,
                                             _stream(stream)), "s2g_inv_fst_real_f32")
 
+    def fst_complex_f32(self, rgrid, igrid, rcoeffs, icoeffs, batch, precision=PREC_BF16X3, stream=None):
+        """COMPLEX data on the split path: the real and imaginary fields through the real-field
+        transform, combined per coefficient (every order written)."""
+        check(self.lib.s2g_fst_complex_f32(self.h, _addr(rgrid), _addr(igrid), _addr(rcoeffs), _addr(icoeffs), batch,
+                                           precision, _stream(stream)), "s2g_fst_complex_f32")
+
+    def inv_fst_complex_f32(self, rcoeffs, icoeffs, rgrid, igrid, batch, precision=PREC_BF16X3, stream=None):
+        check(self.lib.s2g_inv_fst_complex_f32(self.h, _addr(rcoeffs), _addr(icoeffs), _addr(rgrid), _addr(igrid),
+                                               batch, precision, _stream(stream)), "s2g_inv_fst_complex_f32")
+
     def fst_refined(self, grid, rcoeffs, icoeffs, batch, precision=PREC_BF16X3, stream=None):
         """FP64 in/out forward: split contraction plus one FP64-residual refinement step."""
         check(self.lib.s2g_fst_refined(self.h, _addr(grid), _addr(rcoeffs), _addr(icoeffs), batch, precision,

@@ -884,6 +884,7 @@ struct s2g_plan_s {
     Tables* t;
     Scratch work;
     Scratch io;
+    Scratch cx;  // the two real fields' coefficients of COMPLEX split transforms
     cudaStream_t streams[3];
     cudaEvent_t events[6];
 };
@@ -920,6 +921,7 @@ int s2g_plan_destroy(s2g_plan p) {
     for (auto e : p->events) cudaEventDestroy(e);
     p->work.release();
     p->io.release();
+    p->cx.release();
     put_tables(p->t);
     delete p;
     return S2G_OK;
@@ -982,6 +984,7 @@ int s2g_conv(s2g_plan p, const double* rdata, const double* idata, const double*
 int s2g_fst_real_f32(s2g_plan p, const float* grid, float* rc, float* ic, int batch, int precision, void* stream) {
     S2G_TRY(plan_check(p, batch));
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({grid, rc, ic}));
     S2G_TRY(p->work.ensure(split_work_bytes(p->bw, batch)));
     return fst_split(p->t, grid, rc, ic, batch, precision, p->work.ptr, (cudaStream_t)stream);
 }
@@ -990,14 +993,38 @@ int s2g_inv_fst_real_f32(s2g_plan p, const float* rc, const float* ic, float* gr
                          void* stream) {
     S2G_TRY(plan_check(p, batch));
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({grid, rc, ic}));
     S2G_TRY(p->work.ensure(split_work_bytes(p->bw, batch)));
     return inv_fst_split(p->t, rc, ic, grid, batch, precision, p->work.ptr, (cudaStream_t)stream);
+}
+
+int s2g_fst_complex_f32(s2g_plan p, const float* rgrid, const float* igrid, float* rc, float* ic, int batch,
+                        int precision, void* stream) {
+    S2G_TRY(plan_check(p, batch));
+    if (!rgrid || !igrid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({rgrid, igrid, rc, ic}));
+    S2G_TRY(p->work.ensure(split_work_bytes(p->bw, batch)));
+    S2G_TRY(p->cx.ensure(split_complex_bytes(p->bw, batch)));
+    return fst_split_complex(p->t, rgrid, igrid, rc, ic, batch, precision, p->work.ptr, p->cx.ptr,
+                             (cudaStream_t)stream);
+}
+
+int s2g_inv_fst_complex_f32(s2g_plan p, const float* rc, const float* ic, float* rgrid, float* igrid, int batch,
+                            int precision, void* stream) {
+    S2G_TRY(plan_check(p, batch));
+    if (!rgrid || !igrid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({rgrid, igrid, rc, ic}));
+    S2G_TRY(p->work.ensure(split_work_bytes(p->bw, batch)));
+    S2G_TRY(p->cx.ensure(split_complex_bytes(p->bw, batch)));
+    return inv_fst_split_complex(p->t, rc, ic, rgrid, igrid, batch, precision, p->work.ptr, p->cx.ptr,
+                                 (cudaStream_t)stream);
 }
 
 int s2g_fst_refined(s2g_plan p, const double* grid, double* rc, double* ic, int batch, int precision,
                     void* stream) {
     S2G_TRY(plan_check(p, batch));
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({grid, rc, ic}));
     S2G_TRY(p->work.ensure(refine_work_bytes(p->bw, batch)));
     S2G_TRY(p->io.ensure(refine_io_bytes(p->bw, batch)));
     return fst_refined(p->t, grid, rc, ic, batch, precision, p->io.ptr, p->work.ptr, (cudaStream_t)stream);
@@ -1007,6 +1034,7 @@ int s2g_inv_fst_refined(s2g_plan p, const double* rc, const double* ic, double* 
                         void* stream) {
     S2G_TRY(plan_check(p, batch));
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({grid, rc, ic}));
     S2G_TRY(p->work.ensure(refine_work_bytes(p->bw, batch)));
     S2G_TRY(p->io.ensure(refine_io_bytes(p->bw, batch)));
     return inv_fst_refined(p->t, rc, ic, grid, batch, precision, p->io.ptr, p->work.ptr, (cudaStream_t)stream);

@@ -500,6 +500,7 @@ static int group_check(s2g_group g) {
 int s2g_group_fst(s2g_group g, const float* grid, float* rcoeffs, float* icoeffs, void* stream) {
     S2G_TRY(group_check(g));
     if (!grid || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({grid, rcoeffs, icoeffs}));
     const void* p[3] = {grid, rcoeffs, icoeffs};
     return group_run(g, 0, p, 3, (cudaStream_t)stream);
 }
@@ -507,6 +508,7 @@ int s2g_group_fst(s2g_group g, const float* grid, float* rcoeffs, float* icoeffs
 int s2g_group_inv_fst(s2g_group g, const float* rcoeffs, const float* icoeffs, float* grid, void* stream) {
     S2G_TRY(group_check(g));
     if (!grid || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({grid, rcoeffs, icoeffs}));
     const void* p[3] = {rcoeffs, icoeffs, grid};
     return group_run(g, 1, p, 3, (cudaStream_t)stream);
 }
@@ -515,6 +517,7 @@ int s2g_group_fst_inv(s2g_group g, const float* grid, float* rcoeffs, float* ico
                       void* stream) {
     S2G_TRY(group_check(g));
     if (!grid || !rcoeffs || !icoeffs || !grid_out) return fail(S2G_ERR_ARG, "NULL argument");
+    S2G_TRY(check_aligned16({grid, rcoeffs, icoeffs, grid_out}));
     const void* p[4] = {grid, rcoeffs, icoeffs, grid_out};
     return group_run(g, 2, p, 4, (cudaStream_t)stream);
 }

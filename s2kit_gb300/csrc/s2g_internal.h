@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <initializer_list>
 #include <mutex>
 #include <string>
 
@@ -69,6 +70,14 @@ struct Scratch {
     void release();
 };
 
+// The FP32 transforms move samples and coefficients as float4 and through TMA, so their device
+// pointers must be 16-byte aligned (every cudaMalloc pointer is); others are rejected up front.
+inline int check_aligned16(std::initializer_list<const void*> ps) {
+    for (const void* q : ps)
+        if ((uintptr_t)q & 15) return fail(S2G_ERR_ARG, "device pointer %p is not 16-byte aligned", q);
+    return S2G_OK;
+}
+
 // Build / fetch device tables (cached per device, bw, cutoff); the caller gets a reference and
 // returns it with put_tables.
 int get_tables(int bw, int cutoff, Tables** out);
@@ -122,6 +131,12 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
               cudaStream_t st);
 int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int batch, int precision, void* work,
                   cudaStream_t st);
+// COMPLEX data as two real fields (cwork: split_complex_bytes of scratch besides work).
+size_t split_complex_bytes(int bw, int batch);
+int fst_split_complex(Tables* t, const float* rgrid, const float* igrid, float* rc, float* ic, int batch,
+                      int precision, void* work, void* cwork, cudaStream_t st);
+int inv_fst_split_complex(Tables* t, const float* rc, const float* ic, float* rgrid, float* igrid, int batch,
+                          int precision, void* work, void* cwork, cudaStream_t st);
 // Reads (and optionally clears) the device error word of the tensor-core kernels.
 int split_device_status(Tables* t, int clear);
 

@@ -2226,6 +2226,169 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
     return split_inv_tail(t, F, Fc, grid, batch, nullptr, st);
 }
 
+// ---- COMPLEX data (FST_semi_memo.c:146-200, 290-333) as two real fields ----
+// A complex field f = g + i h has real fields g (rdata) and h (idata), so f(l, m) = g(l, m) + i h(l, m)
+// for every order, and the real fields' symmetry g(l, -m) = (-1)^m conj g(l, m) gives the negative
+// orders from the non-negative ones: f(l, -m) = (-1)^m (conj g(l, m) + i conj h(l, m)).  The real
+// path's packed row DFT (two real latitudes per complex FFT) makes the two real transforms cost what
+// one complex transform would: the same FFT, DCT and contraction work per function.
+
+// Order and degree of position j of the coefficient layout (util.c:42-49): orders 0 .. B-1 with
+// l = m .. B-1, then orders -(B-1) .. -1 with l = |m| .. B-1.
+__device__ __forceinline__ void coeff_order_degree(int j, int B, int* m, int* l) {
+    const int nn = B * (B + 1) / 2;
+    if (j < nn) {  // start(m) = m (2B + 1 - m) / 2
+        const float b = 2.f * B + 1.f;
+        int mm = (int)((b - sqrtf(fmaxf(b * b - 8.f * (float)j, 0.f))) * 0.5f);
+        mm = max(0, min(mm, B - 1));
+        while (mm > 0 && mm * (2 * B + 1 - mm) / 2 > j) --mm;
+        while (mm + 1 < B && (mm + 1) * (2 * B - mm) / 2 <= j) ++mm;
+        *m = mm;
+        *l = mm + j - mm * (2 * B + 1 - mm) / 2;
+    } else {  // block k = B-1-|m| starts at k (k+1) / 2 and holds k+1 degrees
+        const int jj = j - nn;
+        int k = (int)((sqrtf(8.f * (float)jj + 1.f) - 1.f) * 0.5f);
+        k = max(0, min(k, B - 2));
+        while (k > 0 && k * (k + 1) / 2 > jj) --k;
+        while (k + 1 <= B - 2 && (k + 1) * (k + 2) / 2 <= jj) ++k;
+        *m = -(B - 1 - k);
+        *l = (B - 1 - k) + jj - k * (k + 1) / 2;
+    }
+}
+
+__device__ __forceinline__ void coeff_next(int B, int* m, int* l) {
+    if (++*l < B) return;
+    if (*m >= 0) {
+        ++*m;
+        if (*m == B) *m = -(B - 1);
+        *l = *m >= 0 ? *m : -*m;
+    } else {
+        ++*m;
+        *l = -*m;
+    }
+}
+
+// Forward: g, h are [batch][B*B] (re then im arrays, each batch*B*B) from the real path; writes
+// f into rc/ic, four consecutive positions per thread (float4 stores).
+__global__ void __launch_bounds__(256) k_cplx_combine(const float* __restrict__ gr, const float* __restrict__ gi,
+                                                      const float* __restrict__ hr, const float* __restrict__ hi,
+                                                      float* __restrict__ rc, float* __restrict__ ic, int B,
+                                                      long long nquads) {
+    const int BB = B * B, qpf = BB / 4;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nquads;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long f = q / qpf;
+        const int j0 = 4 * (int)(q - f * qpf);
+        const size_t base = (size_t)f * BB;
+        int m, l;
+        coeff_order_degree(j0, B, &m, &l);
+        float orr[4], oi[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int am = m >= 0 ? m : -m;
+            const size_t src = base + am * B - (am * (am - 1)) / 2 + (l - am);
+            const float a = __ldg(gr + src), b = __ldg(gi + src), c = __ldg(hr + src), d = __ldg(hi + src);
+            if (m >= 0) {
+                orr[e] = a - d;
+                oi[e] = b + c;
+            } else {
+                const float s = (am & 1) ? -1.f : 1.f;
+                orr[e] = s * (a + d);
+                oi[e] = s * (c - b);
+            }
+            coeff_next(B, &m, &l);
+        }
+        *(float4*)(rc + base + j0) = make_float4(orr[0], orr[1], orr[2], orr[3]);
+        *(float4*)(ic + base + j0) = make_float4(oi[0], oi[1], oi[2], oi[3]);
+    }
+}
+
+// Inverse: from f (all orders) the non-negative orders of g = (f(l,m) + (-1)^m conj f(l,-m)) / 2 and
+// h = (f(l,m) - (-1)^m conj f(l,-m)) / 2i, four consecutive positions per thread.  The real-field
+// inverse reads only the non-negative orders, so the negative-order slots of g and h stay unwritten.
+__global__ void __launch_bounds__(256) k_cplx_split(const float* __restrict__ rc, const float* __restrict__ ic,
+                                                    float* __restrict__ gr, float* __restrict__ gi,
+                                                    float* __restrict__ hr, float* __restrict__ hi, int B,
+                                                    long long nquads) {
+    const int BB = B * B, nn = B * (B + 1) / 2, qpf = nn / 4;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nquads;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long f = q / qpf;
+        const int j0 = 4 * (int)(q - f * qpf);
+        const size_t base = (size_t)f * BB;
+        int m, l;
+        coeff_order_degree(j0, B, &m, &l);
+        const float4 ar = *(const float4*)(rc + base + j0), ai = *(const float4*)(ic + base + j0);
+        const float far_[4] = {ar.x, ar.y, ar.z, ar.w}, fai[4] = {ai.x, ai.y, ai.z, ai.w};
+        float o[4][4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int L = B - 1;
+            const size_t neg = m == 0 ? base + j0 + e
+                                      : base + (L * (L + 3)) / 2 + 1 + ((L - m) * (L - m + 1)) / 2 + (l - m);
+            const float s = (m & 1) ? -1.f : 1.f;
+            const float br = s * __ldg(rc + neg), bi = -s * __ldg(ic + neg);  // (-1)^m conj f(l, -m)
+            o[0][e] = 0.5f * (far_[e] + br);
+            o[1][e] = 0.5f * (fai[e] + bi);
+            o[2][e] = 0.5f * (fai[e] - bi);
+            o[3][e] = -0.5f * (far_[e] - br);
+            coeff_next(B, &m, &l);
+        }
+        *(float4*)(gr + base + j0) = make_float4(o[0][0], o[0][1], o[0][2], o[0][3]);
+        *(float4*)(gi + base + j0) = make_float4(o[1][0], o[1][1], o[1][2], o[1][3]);
+        *(float4*)(hr + base + j0) = make_float4(o[2][0], o[2][1], o[2][2], o[2][3]);
+        *(float4*)(hi + base + j0) = make_float4(o[3][0], o[3][1], o[3][2], o[3][3]);
+    }
+}
+
+size_t split_complex_bytes(int bw, int batch) { return 4 * (size_t)batch * bw * bw * sizeof(float) + 256; }
+
+static int launch_grid_stride(long long n, int* grid) {
+    int dev = 0, nsm = 0;
+    S2G_CUDA(cudaGetDevice(&dev));
+    S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    *grid = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)nsm * 8));
+    return S2G_OK;
+}
+
+int fst_split_complex(Tables* t, const float* rgrid, const float* igrid, float* rc, float* ic, int batch,
+                      int precision, void* work, void* cwork, cudaStream_t st) {
+    const int B = t->bw;
+    const size_t n = (size_t)batch * B * B;
+    float* g = (float*)cwork;
+    float* h = g + 2 * n;
+    S2G_TRY(fst_split(t, rgrid, g, g + n, batch, precision, work, st));
+    S2G_TRY(fst_split(t, igrid, h, h + n, batch, precision, work, st));
+    const long long nq = (long long)n / 4;
+    int grid;
+    S2G_TRY(launch_grid_stride(nq, &grid));
+    ProfScope ps_("cplx_combine", st);
+    k_cplx_combine<<<grid, 256, 0, st>>>(g, g + n, h, h + n, rc, ic, B, nq);
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+int inv_fst_split_complex(Tables* t, const float* rc, const float* ic, float* rgrid, float* igrid, int batch,
+                          int precision, void* work, void* cwork, cudaStream_t st) {
+    int nprod;
+    bool f16;
+    S2G_TRY(check_prec(precision, &nprod, &f16));
+    const int B = t->bw;
+    const size_t n = (size_t)batch * B * B;
+    float* g = (float*)cwork;
+    float* h = g + 2 * n;
+    const long long nq = (long long)batch * (B * (B + 1) / 2) / 4;
+    int grid;
+    S2G_TRY(launch_grid_stride(nq, &grid));
+    {
+        ProfScope ps_("cplx_split", st);
+        k_cplx_split<<<grid, 256, 0, st>>>(rc, ic, g, g + n, h, h + n, B, nq);
+        S2G_CUDA(cudaGetLastError());
+    }
+    S2G_TRY(inv_fst_split(t, g, g + n, rgrid, batch, precision, work, st));
+    return inv_fst_split(t, h, h + n, igrid, batch, precision, work, st);
+}
+
 // Inverse stages after the contraction: REDFT01 (+ sin(theta) for odd m), naive-order
 // recombination, DFT over the orders into the grid (gmap: per-function grid offsets or null).
 int split_inv_tail(Tables* t, float* F, float* Fc, float* grid, int batch, const int64_t* gmap, cudaStream_t st) {
