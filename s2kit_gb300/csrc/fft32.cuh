@@ -264,7 +264,7 @@ struct WarpFFT4 {
             u[WarpFFT<R>::brev(j)] = make_float2(xr[c * XS + P * j + h], xi[c * XS + P * j + h]);
         __syncwarp();  // the exchange planes are free again (callers reuse them)
         RegStages<R, 2>::run(u, sign);
-        if (P > 1) {
+        if constexpr (P > 1) {
             // (c3) T_h[k] = w_32^(h k) Y_h[k], then the P-point DFT across the column's lanes
             if (h) {
 #pragma unroll
@@ -274,8 +274,8 @@ struct WarpFFT4 {
                     u[k] = cmulf(u[k], w);
                 }
             }
-            if (LP >= 1) stage<0>(u, tw, h, sign);
-            if (LP >= 2) stage<LP >= 2 ? 1 : 0>(u, tw, h, sign);
+            stage<0>(u, tw, h, sign);
+            if constexpr (LP >= 2) stage<1>(u, tw, h, sign);
         }
 #pragma unroll
         for (int k = 0; k < R; ++k) v[k] = u[k];

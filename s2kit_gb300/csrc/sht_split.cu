@@ -1241,7 +1241,10 @@ __global__ void __launch_bounds__(kTPB, 2) k_leg_tc(Leg p, uint32_t stage_bytes,
 //   warps 4-7  : epilogue (warp 4+q reads TMEM lanes 32q..32q+31 = accumulator rows, stages
 //                128-column blocks in shared memory, writes them coalesced);
 //   warps 8-15 : A producers (FP32 loads one chunk ahead, split, store into a kNAS-stage ring);
-//   warps 2-3  : no role.
+//   warp 2     : on the tensor-map path, A loader: one TMA per chunk into the FP32 staging ring,
+//                paced by that ring alone, so the A operand (from HBM) runs up to nstg chunks
+//                ahead of the MMAs while the table (from L2) keeps its own nbs-stage ring;
+//   warp 3     : no role.
 // Every mbarrier wait is bounded; on expiry the role records the abort and leaves its loop,
 // the table producer waits (bounded) for its copies in flight, the MMA thread for its MMAs,
 // and the CTA frees TMEM and returns.
@@ -1250,7 +1253,7 @@ static constexpr int kNI = 4;          // item ring entries
 static constexpr int kNAS = 2;         // A stages
 static constexpr int kMaxNBS = 8;      // table stages (upper bound)
 static constexpr int kEpiCols = 64;    // epilogue staging width
-static constexpr int kMaxStg = 4;      // cp.async staging stages of the BF16 A producers (upper bound)
+static constexpr int kMaxStg = 8;      // FP32 staging stages of the BF16 A producers (upper bound)
 static constexpr int kAProd = 256;     // A-producer threads
 static constexpr int kEpi = 128;       // epilogue threads
 static constexpr uint32_t kStgBytes = kAProd * kTasks * 8 * sizeof(float);  // one staging stage (16 KB)
@@ -1530,11 +1533,12 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int s_abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool a_loader = !F16 && p.tma;  // warp 2 issues the A operand's TMA loads
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < kNI; ++i) {
             tc::mbar_init(&item_full[i], 1);
-            tc::mbar_init(&item_empty[i], 1 + kAProd + kEpi);
+            tc::mbar_init(&item_empty[i], 1 + kAProd + kEpi + (a_loader ? 1 : 0));
             tc::mbar_init(&sc_full[i], kAProd);
         }
         for (int i = 0; i < kNAS; ++i) {
@@ -1568,8 +1572,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     if (warp == 0) {
         // ---------------- scheduler + table producer ----------------
         if (lane == 0) {
-            uint32_t bc = 0;   // table chunks issued
-            uint32_t stc = 0;  // A chunks loaded by TMA (tensor-map path)
+            uint32_t bc = 0;  // table chunks issued
             for (int k = 0; !s_abort; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_empty[slot], ((k / kNI) & 1) ^ 1)) {
@@ -1592,20 +1595,35 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                         break;
                     }
                     issue_table<F16>(smem + b_off + s * b_stage, blob, g.NP, n0, rows, c, &b_full[s]);
-                    if (!F16 && p.tma) {
-                        const int ss = (int)(stc % (uint32_t)nstg);
-                        if (!tc::mbar_wait(&stg_empty[ss], ((stc / nstg) & 1) ^ 1)) {
-                            s_abort = 1;
-                            break;
-                        }
-                        issue_a_tma<FWD>(p, e, c, smem + stg_off + (size_t)ss * stg_stride, &stg_full[ss]);
-                        ++stc;
-                    }
                 }
             }
             // copies in flight land before the CTA leaves (immediate on the normal path)
             for (uint32_t j = bc > (uint32_t)nbs ? bc - nbs : 0; j < bc; ++j)
                 tc::mbar_wait(&b_full[j % nbs], (j / nbs) & 1);
+        }
+    } else if (warp == 2 && a_loader) {
+        // ---------------- A loader (tensor-map path) ----------------
+        if (lane == 0) {
+            uint32_t stc = 0;  // A chunks issued
+            for (int k = 0; !s_abort; ++k) {
+                const int slot = k % kNI;
+                if (!tc::mbar_wait(&item_full[slot], (k / kNI) & 1)) {
+                    s_abort = 1;
+                    break;
+                }
+                const WsItem e = items[slot];
+                tc::mbar_arrive(&item_empty[slot]);
+                if (e.ci < 0) break;
+                const int nch = geo(FWD, p.cls[e.ci].B, e.m).nch;
+                for (int c = 0; c < nch; ++c, ++stc) {
+                    const int ss = (int)(stc % (uint32_t)nstg);
+                    if (!tc::mbar_wait(&stg_empty[ss], ((stc / nstg) & 1) ^ 1)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    issue_a_tma<FWD>(p, e, c, smem + stg_off + (size_t)ss * stg_stride, &stg_full[ss]);
+                }
+            }
             for (uint32_t j = stc > (uint32_t)nstg ? stc - nstg : 0; j < stc; ++j)
                 tc::mbar_wait(&stg_full[j % nstg], (j / nstg) & 1);
         }
