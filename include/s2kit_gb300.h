@@ -256,6 +256,21 @@ int s2g_fst_real_f32_host(s2g_plan plan, const float* grid, float* rcoeffs, floa
 int s2g_inv_fst_real_f32_host(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid, int batch,
                               int precision);
 
+/* The same, queued without waiting: each call returns once its copies and transforms are queued
+ * on the plan's streams, so the uploads of one call overlap the downloads of the one before (the
+ * host link carries both directions at once).  Host memory that a queued call reads or writes is
+ * tracked per chunk: a later call's upload from memory an earlier call downloads into waits for
+ * that download, and a later download into memory an earlier call uploads from waits for that
+ * upload, so chained calls on aliased buffers are ordered.  The caller leaves the buffers alone
+ * until s2g_plan_wait returns.  Calls on the plan that take device buffers wait for queued
+ * host-buffer work first (they share its scratch). */
+int s2g_fst_real_f32_host_async(s2g_plan plan, const float* grid, float* rcoeffs, float* icoeffs, int batch,
+                                int precision);
+int s2g_inv_fst_real_f32_host_async(s2g_plan plan, const float* rcoeffs, const float* icoeffs, float* grid,
+                                    int batch, int precision);
+/* Waits for every host-buffer call queued on the plan. */
+int s2g_plan_wait(s2g_plan plan);
+
 /* Waits for the plan's device work and reports a failure recorded on the device by the
  * tensor-core kernels (S2G_ERR_TIMEOUT when a bounded wait expired); clears the record. */
 int s2g_plan_sync_status(s2g_plan plan);

@@ -66,6 +66,9 @@ SIGNATURES = {
     "s2g_inv_fst_real_f32": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, vp]),
     "s2g_fst_real_f32_host": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
     "s2g_inv_fst_real_f32_host": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
+    "s2g_fst_real_f32_host_async": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
+    "s2g_inv_fst_real_f32_host_async": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int]),
+    "s2g_plan_wait": (C.c_int, [vp]),
     "s2g_fst_complex_f32": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
     "s2g_inv_fst_complex_f32": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
     "s2g_plan_sync_status": (C.c_int, [vp]),

@@ -267,6 +267,22 @@ class Plan:
         check(self.lib.s2g_inv_fst_real_f32_host(self.h, rcoeffs.ctypes.data, icoeffs.ctypes.data, grid.ctypes.data,
                                                  batch, precision), "s2g_inv_fst_real_f32_host")
 
+    def fst_real_f32_host_async(self, grid: np.ndarray, rcoeffs: np.ndarray, icoeffs: np.ndarray, batch, precision):
+        """Queued host-buffer forward; the buffers stay in use until wait()."""
+        check(self.lib.s2g_fst_real_f32_host_async(self.h, grid.ctypes.data, rcoeffs.ctypes.data,
+                                                   icoeffs.ctypes.data, batch, precision),
+              "s2g_fst_real_f32_host_async")
+
+    def inv_fst_real_f32_host_async(self, rcoeffs: np.ndarray, icoeffs: np.ndarray, grid: np.ndarray, batch,
+                                    precision):
+        check(self.lib.s2g_inv_fst_real_f32_host_async(self.h, rcoeffs.ctypes.data, icoeffs.ctypes.data,
+                                                       grid.ctypes.data, batch, precision),
+              "s2g_inv_fst_real_f32_host_async")
+
+    def wait(self):
+        """Waits for the host-buffer calls queued on this plan."""
+        check(self.lib.s2g_plan_wait(self.h), "s2g_plan_wait")
+
 
 class Group:
     """Grouped transforms of many real functions of uneven bandwidth (s2g_group_*).

@@ -12,6 +12,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <algorithm>
 #include <vector>
 
 #include "s2g_common.cuh"
@@ -879,6 +880,14 @@ int s2g_cache_clear(void) {
     return S2G_OK;
 }
 
+// A host range that a queued copy of the host-buffer pipeline reads (H2D) or writes (D2H),
+// with the event recorded after that copy.
+struct HostDep {
+    uintptr_t lo, hi;
+    bool write;
+    cudaEvent_t ev;
+};
+
 struct s2g_plan_s {
     int bw, cutoff, device;
     Tables* t;
@@ -887,7 +896,63 @@ struct s2g_plan_s {
     Scratch cx;  // the two real fields' coefficients of COMPLEX split transforms
     cudaStream_t streams[3];
     cudaEvent_t events[6];
+    // host-buffer pipeline state, kept across asynchronous calls
+    std::vector<HostDep> deps;        // queued copies from or into host memory
+    std::vector<cudaEvent_t> ev_free;  // recycled events
+    unsigned long long seq = 0;        // chunks issued; staging buffer = seq & 1
+    size_t stage = 0;                  // bytes of one staging buffer
+    int host_pending = 0;              // host-buffer work may still be queued
 };
+
+// Waits for every queued host-buffer transfer and transform of the plan.
+static int drain_host(s2g_plan p) {
+    if (!p->host_pending) return S2G_OK;
+    for (auto s : p->streams) S2G_CUDA(cudaStreamSynchronize(s));
+    for (auto& d : p->deps) p->ev_free.push_back(d.ev);
+    p->deps.clear();
+    p->host_pending = 0;
+    return S2G_OK;
+}
+
+// Drops the dependencies whose copies have completed.
+static void prune_deps(s2g_plan p) {
+    size_t k = 0;
+    for (auto& d : p->deps) {
+        if (cudaEventQuery(d.ev) == cudaSuccess)
+            p->ev_free.push_back(d.ev);
+        else
+            p->deps[k++] = d;
+    }
+    p->deps.resize(k);
+    if (cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();  // a query's "not yet", not a fault
+}
+
+// Makes stream s wait for the queued copies that conflict with host range [ptr, ptr + bytes):
+// a read waits for earlier writes into the range, a write also for earlier reads out of it.
+static int wait_host_range(s2g_plan p, cudaStream_t s, const void* ptr, size_t bytes, bool write) {
+    const uintptr_t lo = (uintptr_t)ptr, hi = lo + bytes;
+    for (auto& d : p->deps)
+        if (d.lo < hi && lo < d.hi && (write || d.write)) S2G_CUDA(cudaStreamWaitEvent(s, d.ev, 0));
+    return S2G_OK;
+}
+
+// Records that the copy just queued on s reads (or writes) host range [ptr, ptr + bytes).
+static int note_host_range(s2g_plan p, cudaStream_t s, const void* ptr, size_t bytes, bool write) {
+    cudaEvent_t e;
+    if (!p->ev_free.empty()) {
+        e = p->ev_free.back();
+        p->ev_free.pop_back();
+    } else {
+        S2G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const cudaError_t r = cudaEventRecord(e, s);
+    if (r != cudaSuccess) {
+        p->ev_free.push_back(e);
+        return cuda_fail(r, "cudaEventRecord");
+    }
+    p->deps.push_back({(uintptr_t)ptr, (uintptr_t)ptr + bytes, write, e});
+    return S2G_OK;
+}
 
 int s2g_plan_create(s2g_plan* plan, int bw, int cutoff) {
     if (!plan) return fail(S2G_ERR_ARG, "NULL plan pointer");
@@ -919,6 +984,8 @@ int s2g_plan_destroy(s2g_plan p) {
         cudaStreamDestroy(s);
     }
     for (auto e : p->events) cudaEventDestroy(e);
+    for (auto& d : p->deps) cudaEventDestroy(d.ev);
+    for (auto e : p->ev_free) cudaEventDestroy(e);
     p->work.release();
     p->io.release();
     p->cx.release();
@@ -933,12 +1000,15 @@ size_t s2g_plan_workspace_size(s2g_plan p, int batch, int precision) {
     return split_work_bytes(p->bw, batch);
 }
 
-static int plan_check(s2g_plan p, int batch) {
+// Device-buffer calls share the plan's scratch with the host-buffer pipeline, so they first wait
+// for host-buffer work still queued (host = true: the pipeline itself, which orders its own work).
+static int plan_check(s2g_plan p, int batch, bool host = false) {
     if (!p) return fail(S2G_ERR_ARG, "NULL plan");
     if (batch < 1) return fail(S2G_ERR_ARG, "batch %d < 1", batch);
     int dev;
     S2G_TRY(current_device(&dev));
     if (dev != p->device) return fail(S2G_ERR_ARG, "plan made on device %d used on device %d", p->device, dev);
+    if (!host) S2G_TRY(drain_host(p));
     return S2G_OK;
 }
 
@@ -1043,44 +1113,67 @@ int s2g_inv_fst_refined(s2g_plan p, const double* rc, const double* ic, double* 
 int s2g_plan_sync_status(s2g_plan p) {
     if (!p) return fail(S2G_ERR_ARG, "NULL plan");
     S2G_CUDA(cudaSetDevice(p->device));
+    S2G_TRY(drain_host(p));
     S2G_CUDA(cudaDeviceSynchronize());
     return split_device_status(p->t, 1);
 }
 
 // Host-buffer variants: chunks of the batch flow H2D (stream 0) -> compute (stream 1) -> D2H
-// (stream 2) through double-buffered device staging, so copies overlap the transforms.
+// (stream 2) through double-buffered device staging, so copies overlap the transforms.  The
+// staging buffers, their events and the chunk sequence live in the plan, so an asynchronous call
+// queues behind the previous one and its uploads overlap the previous call's downloads.  Copies
+// from or into host memory that a queued copy of an earlier call writes or reads wait for it
+// (per chunk, through the plan's list of queued host ranges).
 static int host_pipeline(s2g_plan p, int fwd, const float* in0, const float* in1, float* out0, float* out1,
-                         int batch, int precision) {
-    S2G_TRY(plan_check(p, batch));
+                         int batch, int precision, bool async) {
+    S2G_TRY(plan_check(p, batch, true));
     const size_t S = 2 * (size_t)p->bw, ng = S * S, nc = (size_t)p->bw * p->bw;
     const size_t in_per = fwd ? ng : 2 * nc, out_per = fwd ? 2 * nc : ng;
     int chunk = batch < 32 ? batch : 32;  // short fill and drain: the first upload and last download do not overlap
     while (chunk > 1 && (size_t)chunk * (in_per + out_per) * 4 * 2 > ((size_t)4 << 30)) chunk /= 2;
-    const size_t in_b = (size_t)chunk * in_per * 4, out_b = (size_t)chunk * out_per * 4;
-    S2G_TRY(p->io.ensure(2 * (in_b + out_b) + 1024));
-    S2G_TRY(p->work.ensure(split_work_bytes(p->bw, chunk)));
+    // one staging layout for both directions, so queued chunks of an earlier call keep their buffers
+    const size_t stage = (size_t)chunk * std::max(ng, 2 * nc) * 4;
+    if (stage != p->stage || p->io.bytes < 4 * stage + 1024 || p->work.bytes < split_work_bytes(p->bw, chunk)) {
+        S2G_TRY(drain_host(p));  // a new layout or a larger buffer: nothing queued may still use the old one
+        S2G_TRY(p->io.ensure(4 * stage + 1024));
+        S2G_TRY(p->work.ensure(split_work_bytes(p->bw, chunk)));
+        p->stage = stage;
+    }
+    prune_deps(p);
+    if (p->deps.size() > 4096) S2G_TRY(drain_host(p));
     char* base = (char*)p->io.ptr;
-    float* din[2] = {(float*)base, (float*)(base + in_b)};
-    float* dout[2] = {(float*)(base + 2 * in_b), (float*)(base + 2 * in_b + out_b)};
+    float* din[2] = {(float*)base, (float*)(base + stage)};
+    float* dout[2] = {(float*)(base + 2 * stage), (float*)(base + 3 * stage)};
     cudaStream_t h2d = p->streams[0], comp = p->streams[1], d2h = p->streams[2];
     cudaEvent_t in_ready[2] = {p->events[0], p->events[1]};
     cudaEvent_t done[2] = {p->events[2], p->events[3]};
     cudaEvent_t out_free[2] = {p->events[4], p->events[5]};
+    p->host_pending = 1;
     const int nchunks = (batch + chunk - 1) / chunk;
     for (int c = 0; c < nchunks; ++c) {
-        const int b = c & 1;
+        const int b = (int)(p->seq++ & 1);
         const int f0 = c * chunk, n = (batch - f0 < chunk) ? batch - f0 : chunk;
-        if (c >= 2) S2G_CUDA(cudaStreamWaitEvent(h2d, done[b], 0));  // compute of c-2 consumed din[b]
+        S2G_CUDA(cudaStreamWaitEvent(h2d, done[b], 0));  // the transform that last read din[b]
         if (fwd) {
-            S2G_CUDA(cudaMemcpyAsync(din[b], in0 + (size_t)f0 * ng, (size_t)n * ng * 4, cudaMemcpyHostToDevice, h2d));
+            const float* src = in0 + (size_t)f0 * ng;
+            const size_t by = (size_t)n * ng * 4;
+            S2G_TRY(wait_host_range(p, h2d, src, by, false));
+            S2G_CUDA(cudaMemcpyAsync(din[b], src, by, cudaMemcpyHostToDevice, h2d));
+            S2G_TRY(note_host_range(p, h2d, src, by, false));
         } else {
-            S2G_CUDA(cudaMemcpyAsync(din[b], in0 + (size_t)f0 * nc, (size_t)n * nc * 4, cudaMemcpyHostToDevice, h2d));
-            S2G_CUDA(cudaMemcpyAsync(din[b] + (size_t)n * nc, in1 + (size_t)f0 * nc, (size_t)n * nc * 4,
-                                     cudaMemcpyHostToDevice, h2d));
+            const size_t by = (size_t)n * nc * 4;
+            const float* s0 = in0 + (size_t)f0 * nc;
+            const float* s1 = in1 + (size_t)f0 * nc;
+            S2G_TRY(wait_host_range(p, h2d, s0, by, false));
+            S2G_TRY(wait_host_range(p, h2d, s1, by, false));
+            S2G_CUDA(cudaMemcpyAsync(din[b], s0, by, cudaMemcpyHostToDevice, h2d));
+            S2G_CUDA(cudaMemcpyAsync(din[b] + (size_t)n * nc, s1, by, cudaMemcpyHostToDevice, h2d));
+            S2G_TRY(note_host_range(p, h2d, s0, by, false));
+            S2G_TRY(note_host_range(p, h2d, s1, by, false));
         }
         S2G_CUDA(cudaEventRecord(in_ready[b], h2d));
         S2G_CUDA(cudaStreamWaitEvent(comp, in_ready[b], 0));
-        if (c >= 2) S2G_CUDA(cudaStreamWaitEvent(comp, out_free[b], 0));  // D2H of c-2 read dout[b]
+        S2G_CUDA(cudaStreamWaitEvent(comp, out_free[b], 0));  // the download that last read dout[b]
         if (fwd)
             S2G_TRY(fst_split(p->t, din[b], dout[b], dout[b] + (size_t)n * nc, n, precision, p->work.ptr, comp));
         else
@@ -1088,26 +1181,52 @@ static int host_pipeline(s2g_plan p, int fwd, const float* in0, const float* in1
         S2G_CUDA(cudaEventRecord(done[b], comp));
         S2G_CUDA(cudaStreamWaitEvent(d2h, done[b], 0));
         if (fwd) {
-            S2G_CUDA(cudaMemcpyAsync(out0 + (size_t)f0 * nc, dout[b], (size_t)n * nc * 4, cudaMemcpyDeviceToHost, d2h));
-            S2G_CUDA(cudaMemcpyAsync(out1 + (size_t)f0 * nc, dout[b] + (size_t)n * nc, (size_t)n * nc * 4,
-                                     cudaMemcpyDeviceToHost, d2h));
+            const size_t by = (size_t)n * nc * 4;
+            float* o0 = out0 + (size_t)f0 * nc;
+            float* o1 = out1 + (size_t)f0 * nc;
+            S2G_TRY(wait_host_range(p, d2h, o0, by, true));
+            S2G_TRY(wait_host_range(p, d2h, o1, by, true));
+            S2G_CUDA(cudaMemcpyAsync(o0, dout[b], by, cudaMemcpyDeviceToHost, d2h));
+            S2G_CUDA(cudaMemcpyAsync(o1, dout[b] + (size_t)n * nc, by, cudaMemcpyDeviceToHost, d2h));
+            S2G_TRY(note_host_range(p, d2h, o0, by, true));
+            S2G_TRY(note_host_range(p, d2h, o1, by, true));
         } else {
-            S2G_CUDA(cudaMemcpyAsync(out0 + (size_t)f0 * ng, dout[b], (size_t)n * ng * 4, cudaMemcpyDeviceToHost, d2h));
+            const size_t by = (size_t)n * ng * 4;
+            float* o0 = out0 + (size_t)f0 * ng;
+            S2G_TRY(wait_host_range(p, d2h, o0, by, true));
+            S2G_CUDA(cudaMemcpyAsync(o0, dout[b], by, cudaMemcpyDeviceToHost, d2h));
+            S2G_TRY(note_host_range(p, d2h, o0, by, true));
         }
         S2G_CUDA(cudaEventRecord(out_free[b], d2h));
     }
-    S2G_CUDA(cudaStreamSynchronize(d2h));
-    return S2G_OK;
+    return async ? S2G_OK : drain_host(p);
 }
 
 int s2g_fst_real_f32_host(s2g_plan p, const float* grid, float* rc, float* ic, int batch, int precision) {
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
-    return host_pipeline(p, 1, grid, nullptr, rc, ic, batch, precision);
+    return host_pipeline(p, 1, grid, nullptr, rc, ic, batch, precision, false);
 }
 
 int s2g_inv_fst_real_f32_host(s2g_plan p, const float* rc, const float* ic, float* grid, int batch, int precision) {
     if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
-    return host_pipeline(p, 0, rc, ic, grid, nullptr, batch, precision);
+    return host_pipeline(p, 0, rc, ic, grid, nullptr, batch, precision, false);
+}
+
+int s2g_fst_real_f32_host_async(s2g_plan p, const float* grid, float* rc, float* ic, int batch, int precision) {
+    if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    return host_pipeline(p, 1, grid, nullptr, rc, ic, batch, precision, true);
+}
+
+int s2g_inv_fst_real_f32_host_async(s2g_plan p, const float* rc, const float* ic, float* grid, int batch,
+                                    int precision) {
+    if (!grid || !rc || !ic) return fail(S2G_ERR_ARG, "NULL argument");
+    return host_pipeline(p, 0, rc, ic, grid, nullptr, batch, precision, true);
+}
+
+int s2g_plan_wait(s2g_plan p) {
+    if (!p) return fail(S2G_ERR_ARG, "NULL plan");
+    S2G_CUDA(cudaSetDevice(p->device));
+    return drain_host(p);
 }
 
 int s2g_prof_enable(int on) {
