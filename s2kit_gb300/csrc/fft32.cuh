@@ -309,4 +309,68 @@ struct WarpFFTSel<16> : WarpFFT4<16> {};
 template <>
 struct WarpFFTSel<32> : WarpFFT4<32> {};
 
+// Length 2048 (R = 64) in one warp as two four-step FFTs of length 1024 (the even and the odd
+// samples, 32 values per lane each, so the lane's registers hold half of what a 64-value
+// transform needs) and one radix-2 decimation-in-time step:
+//   X[k] = E[k] + w^k O[k],  X[k + 1024] = E[k] - w^k O[k],  w = exp(sign 2 pi i / 2048), k < 1024.
+// The spectrum is left in the warp's padded buffer zr/zi[pad32(k)], k < 2048 (at least pad32(2048)
+// floats per plane).  The even pass exchanges in [0, 1056) and leaves E there; the odd pass
+// exchanges in [1056, 2112); each (lane, register) then reads back the E value it stored itself.
+// Tables: tw and twb of the length-1024 transform (see WarpFFT4), twc[k] = exp(2 pi i k / 2048).
+struct WarpFFT2048 {
+    static constexpr int H = 1024, OFF = 1056;
+    __device__ __forceinline__ static void store_even(const float2 (&v)[32], float* zr, float* zi) {
+#pragma unroll
+        for (int k1 = 0; k1 < 32; ++k1) {
+            const int o = pad32(WarpFFT4<32>::out_index(k1));
+            zr[o] = v[k1].x;
+            zi[o] = v[k1].y;
+        }
+    }
+    __device__ __forceinline__ static void combine(const float2 (&v)[32], const float2* __restrict__ twc, float* zr,
+                                                   float* zi, float sign) {
+#pragma unroll
+        for (int k1 = 0; k1 < 32; ++k1) {
+            const int k = WarpFFT4<32>::out_index(k1);
+            float2 w = twc[k];
+            w.y *= sign;
+            const float2 o = cmulf(v[k1], w);
+            const int p0 = pad32(k), p1 = pad32(k + H);
+            const float er = zr[p0], ei = zi[p0];
+            zr[p0] = er + o.x;
+            zi[p0] = ei + o.y;
+            zr[p1] = er - o.x;
+            zi[p1] = ei - o.y;
+        }
+    }
+    // in(j): the complex input sample j < 2048 (read twice per call: even j, then odd j)
+    template <class In>
+    __device__ __forceinline__ static void to_spectrum(In in, const float2* __restrict__ tw,
+                                                       const float2* __restrict__ twb, const float2* __restrict__ twc,
+                                                       float* zr, float* zi, float sign) {
+        const int lane = threadIdx.x & 31;
+        float2 v[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = in(2 * (lane + 32 * i));
+        WarpFFT4<32>::run(v, tw, twb, zr, zi, sign);
+        store_even(v, zr, zi);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = in(2 * (lane + 32 * i) + 1);
+        WarpFFT4<32>::run(v, tw, twb, zr + OFF, zi + OFF, sign);
+        combine(v, twc, zr, zi, sign);
+    }
+    // the same with both halves' inputs already in registers (ve: even samples, vo: odd samples,
+    // lane + 32 i each); vo is overwritten
+    __device__ __forceinline__ static void to_spectrum_regs(float2 (&ve)[32], float2 (&vo)[32],
+                                                            const float2* __restrict__ tw,
+                                                            const float2* __restrict__ twb,
+                                                            const float2* __restrict__ twc, float* zr, float* zi,
+                                                            float sign) {
+        WarpFFT4<32>::run(ve, tw, twb, zr, zi, sign);
+        store_even(ve, zr, zi);
+        WarpFFT4<32>::run(vo, tw, twb, zr + OFF, zi + OFF, sign);
+        combine(vo, twc, zr, zi, sign);
+    }
+};
+
 }  // namespace s2g

@@ -407,11 +407,22 @@ __device__ __forceinline__ void load_tw(float2* tw, float2* twb, float2* twD, co
     }
 }
 
+// Tables of the length-2048 transforms (R = 64), which run as two length-1024 four-step FFTs and
+// a radix-2 step (WarpFFT2048): tw[padtw(k)] = exp(2 pi i k / 1024), its (register, lane) copy twb,
+// and twc[k] = exp(2 pi i k / 2048), k < 1024; gS is the length-2048 table.
+__device__ __forceinline__ void load_tw_split(float2* tw, float2* twb, float2* twc, const float2* gS) {
+    for (int k = threadIdx.x; k < 1024; k += blockDim.x) {
+        tw[padtw(k)] = gS[2 * k];
+        twb[k] = gS[2 * (((k & 31) * (k >> 5)) & 1023)];
+        twc[k] = gS[k];
+    }
+}
+
 // CTA shape of the FFT kernels: W warps (one sequence each), LAT = 2W latitudes per CTA in the
-// row kernels.  S = 2048 (R = 64) halves the warps so that the staging fits in shared memory.
+// row kernels.  At S = 2048 (R = 64) one such CTA takes 170-195 KB of shared memory (one per SM).
 template <int R>
 struct FftShape {
-    static constexpr int W = R >= 64 ? 4 : 8;
+    static constexpr int W = 8;
     static constexpr int LAT = 2 * W;
     static constexpr int T = 32 * W;
 };
@@ -429,6 +440,8 @@ struct FftSmem {
     static constexpr int TS = FftShape<R>::LAT + 1;              // rows-inverse tile row (odd)
     // the four-step warp FFT exchanges through the warp's spectrum rows
     static_assert((R != 8 && R != 16 && R != 32) || R * (32 + 32 / R) <= PSA, "exchange planes fit the spectrum rows");
+    // R = 64 (WarpFFT2048): the odd pass exchanges in [OFF, OFF + 32 * 33), the spectrum reaches pad32(2047)
+    static_assert(R != 64 || (WarpFFT2048::OFF + 32 * 33 <= PSA && pad32(S - 1) < PSA), "split 2048 buffers fit");
 };
 
 // DFT along phi of LAT latitudes (two real rows per warp), transposed to X[p][f][m][theta], m < B.
@@ -447,28 +460,34 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
     float* spr = fsm;                  // [W][PSA] re
     float* spi = spr + W * PSA;        // [W][PSA] im
     float2* tw = reinterpret_cast<float2*>(spi + W * PSA);
-    float2* twb = tw + twtab_len(S);
+    float2* twb = tw + (R == 64 ? twtab_len(S / 2) : twtab_len(S));
+    float2* twc = twb + S / 2;  // R = 64 only
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    load_tw(tw, twb, nullptr, gtw, nullptr, S);
+    if constexpr (R == 64)
+        load_tw_split(tw, twb, twc, gtw);
+    else
+        load_tw(tw, twb, nullptr, gtw, nullptr, S);
     __syncthreads();
     // CTA-strided (function, latitude block) tiles; launched with one tile per CTA
     constexpr int NLB = S / LAT;
     for (int tile = blockIdx.x; tile < N * NLB; tile += gridDim.x) {
     const int f = tile / NLB, th0 = (tile - f * NLB) * LAT;
-    float2 v[R];
-    {
-        const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + 2 * warp) * S;
-#pragma unroll
-        for (int i = 0; i < R; ++i) v[i] = make_float2(ra[lane + 32 * i], ra[S + lane + 32 * i]);
-    }
+    const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + 2 * warp) * S;
     float* wr = spr + warp * PSA;
     float* wi = spi + warp * PSA;
-    WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
+    if constexpr (R == 64) {
+        WarpFFT2048::to_spectrum([&](int j) { return make_float2(ra[j], ra[S + j]); }, tw, twb, twc, wr, wi, -1.f);
+    } else {
+        float2 v[R];
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) {
-        const int o = pad32(WarpFFTSel<R>::out_index(k1));
-        wr[o] = v[k1].x;
-        wi[o] = v[k1].y;
+        for (int i = 0; i < R; ++i) v[i] = make_float2(ra[lane + 32 * i], ra[S + lane + 32 * i]);
+        WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) {
+            const int o = pad32(WarpFFTSel<R>::out_index(k1));
+            wr[o] = v[k1].x;
+            wi[o] = v[k1].y;
+        }
     }
     __syncthreads();
     const size_t plane = (size_t)N * B * S;
@@ -514,8 +533,12 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
     float* w = spi + W * PSA;          // 2S weights (even orders, then odd)
     float2* twP = reinterpret_cast<float2*>(w + 2 * S);  // B output twiddles, see below
     float2* tw = twP + B;
-    float2* twb = tw + twtab_len(S);
-    load_tw(tw, twb, nullptr, gtw, nullptr, S);
+    float2* twb = tw + (R == 64 ? twtab_len(S / 2) : twtab_len(S));
+    float2* twc = twb + S / 2;  // R = 64 only
+    if constexpr (R == 64)
+        load_tw_split(tw, twb, twc, gtw);
+    else
+        load_tw(tw, twb, nullptr, gtw, nullptr, S);
     // (cos, sin)(pi k / 2S) of output o (k = 2o, or 2(o - B/2) + 1 for o >= B/2), stored at
     // (o % 4) B/4 + o / 4: the output loop's lanes (4 consecutive o each) read consecutive entries
     for (int o = threadIdx.x; o < B; o += blockDim.x)
@@ -553,19 +576,23 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
         continue;
     }
     const float* ws = w + ((m & 1) ? S : 0);
-    float2 v[R];
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-        const int j = lane + 32 * i;                        // v[j] = x[2j] | x[2(S-1-j)+1]
+    auto in = [&](int j) {  // v[j] = x[2j] | x[2(S-1-j)+1]
         const int q = (j < S / 2) ? 2 * j : 2 * (S - 1 - j) + 1;
-        v[i] = make_float2(xr[q] * ws[q], xi[q] * ws[q]);
-    }
-    WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
+        return make_float2(xr[q] * ws[q], xi[q] * ws[q]);
+    };
+    if constexpr (R == 64) {
+        WarpFFT2048::to_spectrum(in, tw, twb, twc, wr, wi, -1.f);
+    } else {
+        float2 v[R];
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) {
-        const int o = pad32(WarpFFTSel<R>::out_index(k1));
-        wr[o] = v[k1].x;
-        wi[o] = v[k1].y;
+        for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
+        WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) {
+            const int o = pad32(WarpFFTSel<R>::out_index(k1));
+            wr[o] = v[k1].x;
+            wi[o] = v[k1].y;
+        }
     }
     __syncwarp();
     const float nrm = rsqrtf(2.f * S);
@@ -612,8 +639,14 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     float* sn = spi + W * PSA;         // S
     float2* twD = reinterpret_cast<float2*>(sn + S);
     float2* tw = twD + S;
-    float2* twb = tw + twtab_len(S);
-    load_tw(tw, twb, twD, gtw, gtwD, S);
+    float2* twb = tw + (R == 64 ? twtab_len(S / 2) : twtab_len(S));
+    float2* twc = twb + S / 2;  // R = 64 only
+    if constexpr (R == 64) {
+        load_tw_split(tw, twb, twc, gtw);
+        for (int k = threadIdx.x; k < S; k += blockDim.x) twD[k] = gtwD[k];
+    } else {
+        load_tw(tw, twb, twD, gtw, gtwD, S);
+    }
     for (int q = threadIdx.x; q < S; q += blockDim.x) sn[q] = gsin[q];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -653,24 +686,28 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     // Fc[p][f][m][t][j]: cosine coefficient k = 2j + t at (k & 1) * B/2 + k/2
     const float* xa = Fc + (size_t)row * B;
     const float* xb = Fc + (size_t)(nrows + row) * B;
-    float2 v[R];
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-        const int k = lane + 32 * i;
+    auto in = [&](int k) {
         const int r = S - k;
         const int ok = (k & 1) * (B / 2) + (k >> 1), orr = (r & 1) * (B / 2) + (r >> 1);
         const float ak = (k < B) ? xa[ok] : 0.f, bk = (k < B) ? xb[ok] : 0.f;
         const float ar = (k > 0 && r < B) ? xa[orr] : 0.f, br = (k > 0 && r < B) ? xb[orr] : 0.f;
         const float wr = ak + br, wi = bk - ar;
         const float2 d = twD[k];
-        v[i] = make_float2(wr * d.x - wi * d.y, wr * d.y + wi * d.x);
-    }
-    WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
+        return make_float2(wr * d.x - wi * d.y, wr * d.y + wi * d.x);
+    };
+    if constexpr (R == 64) {
+        WarpFFT2048::to_spectrum(in, tw, twb, twc, zr, zi, 1.f);
+    } else {
+        float2 v[R];
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) {
-        const int o = pad32(WarpFFTSel<R>::out_index(k1));
-        zr[o] = v[k1].x;
-        zi[o] = v[k1].y;
+        for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
+        WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) {
+            const int o = pad32(WarpFFTSel<R>::out_index(k1));
+            zr[o] = v[k1].x;
+            zi[o] = v[k1].y;
+        }
     }
     __syncwarp();
     float* fr = F + (size_t)row * S;
@@ -714,9 +751,13 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
     float* spr = fsm;
     float* spi = spr + W * PSA;
     float2* tw = reinterpret_cast<float2*>(fsm + U);
-    float2* twb = tw + twtab_len(S);
+    float2* twb = tw + (R == 64 ? twtab_len(S / 2) : twtab_len(S));
+    float2* twc = twb + S / 2;  // R = 64 only
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    load_tw(tw, twb, nullptr, gtw, nullptr, S);
+    if constexpr (R == 64)
+        load_tw_split(tw, twb, twc, gtw);
+    else
+        load_tw(tw, twb, nullptr, gtw, nullptr, S);
     const size_t plane = (size_t)N * B * S;
     // CTA-strided (function, latitude block) tiles; launched with one tile per CTA
     constexpr int NLB = S / LAT;
@@ -751,10 +792,7 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
     }
     __syncthreads();
     const int a = 2 * warp, b = a + 1;
-    float2 v[R];
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-        const int m = lane + 32 * i;
+    auto in = [&](int m) {
         float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
         if (m < B) {
             ar = tr[m * TS + a];
@@ -768,17 +806,32 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
             br = tr[mm * TS + b];
             bi = -ti[mm * TS + b];
         }
-        v[i] = make_float2(ar - bi, ai + br);  // F_a + i F_b
-    }
-    __syncthreads();  // the tile is dead: spectrum buffers below overwrite it
+        return make_float2(ar - bi, ai + br);  // F_a + i F_b
+    };
     float* zr = spr + warp * PSA;
     float* zi = spi + warp * PSA;
-    WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
+    if constexpr (R == 64) {
+        // both halves' inputs are gathered before the tile dies (its space becomes the spectra)
+        float2 ve[32], vo[32];
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) {
-        const int o = pad32(WarpFFTSel<R>::out_index(k1));
-        zr[o] = v[k1].x;
-        zi[o] = v[k1].y;
+        for (int i = 0; i < 32; ++i) {
+            ve[i] = in(2 * (lane + 32 * i));
+            vo[i] = in(2 * (lane + 32 * i) + 1);
+        }
+        __syncthreads();  // the tile is dead: spectrum buffers below overwrite it
+        WarpFFT2048::to_spectrum_regs(ve, vo, tw, twb, twc, zr, zi, 1.f);
+    } else {
+        float2 v[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
+        __syncthreads();  // the tile is dead: spectrum buffers below overwrite it
+        WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
+#pragma unroll
+        for (int k1 = 0; k1 < R; ++k1) {
+            const int o = pad32(WarpFFTSel<R>::out_index(k1));
+            zr[o] = v[k1].x;
+            zi[o] = v[k1].y;
+        }
     }
     __syncwarp();
     float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;

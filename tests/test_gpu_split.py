@@ -110,6 +110,29 @@ def test_split_matches_oracle_and_roundtrip(oracle):
         assert d <= 2e-6 * mag
 
 
+@pytest.mark.parametrize("nb", [2, 17])
+def test_split_bw1024_forward_inverse_vs_fp64(nb):
+    """bw 1024 (2048-point transforms as two 1024-point four-step FFTs and a radix-2 step)."""
+    torch = _torch()
+    bw = 1024
+    rng = np.random.default_rng(1024 + nb)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    grid64, frc64, fic64 = _fp64_pair(plan, rc, ic)
+    s_rc = torch.full((nb, bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+    s_ic = torch.full_like(s_rc, float("nan"))
+    plan.fst_real_f32(grid64.float(), s_rc, s_ic, nb, api.PREC_BF16X3)
+    s_grid = torch.full((nb, 4 * bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda(), s_grid, nb,
+                          api.PREC_BF16X3)
+    torch.cuda.synchronize()
+    plan.sync_status()
+    mag = torch.hypot(frc64, fic64).amax(dim=1)
+    e_f = (torch.hypot(s_rc.double() - frc64, s_ic.double() - fic64).amax(dim=1) / mag).max().item()
+    e_i = _nerr(s_grid, grid64)
+    assert e_f <= 2e-6 and e_i <= 2e-6, (e_f, e_i)
+
+
 def test_split_host_api_matches_device_api():
     torch = _torch()
     bw, nb = 64, 150  # several pipeline chunks
