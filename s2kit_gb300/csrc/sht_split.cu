@@ -1482,6 +1482,8 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
     constexpr uint32_t kAStage = 3 * kATile;
     const unsigned full = 0xffffffffu;
     uint32_t ac = 0, sc = 0;  // A tiles produced, staging chunks consumed
+    int ss = 0;               // staging stage of chunk sc (running: no division per chunk)
+    uint32_t sph = 0;         // its phase parity
     float one[kTasks];
 #pragma unroll
     for (int q = 0; q < kTasks; ++q) one[q] = 1.f;
@@ -1501,8 +1503,7 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
         const int base = FWD ? 0 : index_of_harmonic_coeff(m, m, B);
         bool ok = true;
         for (int c = 0; c < nch; ++c, ++ac, ++sc) {
-            const int ss = (int)(sc % (uint32_t)nstg);
-            if (!tc::mbar_wait(&stg_full[ss], (sc / nstg) & 1)) {
+            if (!tc::mbar_wait(&stg_full[ss], sph)) {
                 ok = false;
                 break;
             }
@@ -1536,7 +1537,14 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
                     }
                 }
             }
+            // the next chunk's TMA (async proxy) overwrites this staging buffer once the release
+            // below is seen: order this thread's generic-proxy reads of it before that write
+            tc::fence_proxy_async_smem();
             tc::mbar_arrive(&stg_empty[ss]);
+            if (++ss == nstg) {
+                ss = 0;
+                sph ^= 1;
+            }
             const int s = ac % kNAS;
             if (!tc::mbar_wait(&a_empty[s], ((ac / kNAS) & 1) ^ 1)) {
                 ok = false;
@@ -1567,6 +1575,22 @@ __device__ __forceinline__ void issue_a_tma(const Leg& p, const WsItem& e, int c
         tc::tma_load_2d(dst, &p.tmA0, x0, e.f0, bar);
         tc::tma_load_2d(dst + 64 * kInvBox * sizeof(float), &p.tmA1, x0, e.f0, bar);
     }
+}
+
+// The MMAs of one 32-deep chunk: for each 16-deep step, the products x_a t_b of the split terms
+// (lead x0 t0 into the accumulator at d0, the rest into the correction accumulator at d0 + corr);
+// a first chunk starts both accumulators.
+template <int NP>
+__device__ __forceinline__ void mma_chunk(uint32_t d0, uint32_t corr, uint64_t da0, uint64_t db0, uint64_t bstep,
+                                          uint32_t idesc, bool first_chunk) {
+    constexpr int PA[6] = {0, 0, 1, 0, 1, 2}, PB[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+    for (int ks = 0; ks < kKC / 16; ++ks)
+#pragma unroll
+        for (int pr = 0; pr < NP; ++pr)
+            tc::mma_bf16(d0 + (pr ? corr : 0u), da0 + (uint64_t)((PA[pr] * kATile + ks * 256) >> 4),
+                         db0 + PB[pr] * bstep + (uint64_t)((ks * 256) >> 4), idesc,
+                         (first_chunk && ks == 0 && pr <= 1) ? 0u : 1u);
 }
 
 template <bool FWD, bool F16>
@@ -1626,6 +1650,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
         // ---------------- scheduler + table producer ----------------
         if (lane == 0) {
             uint32_t bc = 0;  // table chunks issued
+            int bs = 0;       // stage of chunk bc (running: no division per chunk)
+            uint32_t bph = 0; // its phase parity
             for (int k = 0; !s_abort; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_empty[slot], ((k / kNI) & 1) ^ 1)) {
@@ -1642,12 +1668,15 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 const uint8_t* blob =
                     K.blob + K.blob_off[e.m] + (size_t)(e.t * g.nblk + e.nb) * g.nch * NT * g.NP * kKC * 2;
                 for (int c = 0; c < g.nch; ++c, ++bc) {
-                    const int s = bc % nbs;
-                    if (!tc::mbar_wait(&b_empty[s], ((bc / nbs) & 1) ^ 1)) {
+                    if (!tc::mbar_wait(&b_empty[bs], bph ^ 1)) {
                         s_abort = 1;
                         break;
                     }
-                    issue_table<F16>(smem + b_off + s * b_stage, blob, g.NP, n0, rows, c, &b_full[s]);
+                    issue_table<F16>(smem + b_off + bs * b_stage, blob, g.NP, n0, rows, c, &b_full[bs]);
+                    if (++bs == nbs) {
+                        bs = 0;
+                        bph ^= 1;
+                    }
                 }
             }
             // copies in flight land before the CTA leaves (immediate on the normal path)
@@ -1658,6 +1687,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
         // ---------------- A loader (tensor-map path) ----------------
         if (lane == 0) {
             uint32_t stc = 0;  // A chunks issued
+            int ss = 0;        // stage of chunk stc (running: no division per chunk)
+            uint32_t sph = 0;  // its phase parity
             for (int k = 0; !s_abort; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_full[slot], (k / kNI) & 1)) {
@@ -1669,12 +1700,15 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 if (e.ci < 0) break;
                 const int nch = geo(FWD, p.cls[e.ci].B, e.m).nch;
                 for (int c = 0; c < nch; ++c, ++stc) {
-                    const int ss = (int)(stc % (uint32_t)nstg);
-                    if (!tc::mbar_wait(&stg_empty[ss], ((stc / nstg) & 1) ^ 1)) {
+                    if (!tc::mbar_wait(&stg_empty[ss], sph ^ 1)) {
                         s_abort = 1;
                         break;
                     }
                     issue_a_tma<FWD>(p, e, c, smem + stg_off + (size_t)ss * stg_stride, &stg_full[ss]);
+                    if (++ss == nstg) {
+                        ss = 0;
+                        sph ^= 1;
+                    }
                 }
             }
             for (uint32_t j = stc > (uint32_t)nstg ? stc - nstg : 0; j < stc; ++j)
@@ -1683,7 +1717,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            uint32_t ac = 0, bc = 0;
+            uint32_t ac = 0;            // A chunks consumed
+            int sb = 0;                 // table stage (running, no division per chunk)
+            uint32_t bph = 0;           // its phase parity
             for (int k = 0; !s_abort; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_full[slot], (k / kNI) & 1)) {
@@ -1706,25 +1742,33 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 tc::tc_fence_after();
                 const uint32_t d0 = tmem + buf * accw;
                 bool ok = true;
-                for (int c = 0; c < g.nch; ++c, ++ac, ++bc) {
-                    const int sa = ac % kNAS, sb = bc % nbs;
-                    if (!tc::mbar_wait(&a_full[sa], (ac / kNAS) & 1) || !tc::mbar_wait(&b_full[sb], (bc / nbs) & 1)) {
+                for (int c = 0; c < g.nch; ++c, ++ac) {
+                    const int sa = ac % kNAS;
+                    if (!tc::mbar_wait(&a_full[sa], (ac / kNAS) & 1) || !tc::mbar_wait(&b_full[sb], bph)) {
                         ok = false;
                         break;
                     }
                     tc::tc_fence_after();
                     const uint32_t sa_addr = tc::smem_u32(smem + sa * kAStage);
                     const uint32_t sb_addr = tc::smem_u32(smem + b_off + sb * b_stage);
-                    for (int ks = 0; ks < kKC / 16; ++ks) {
-                        for (int pr = 0; pr < p.nprod; ++pr) {
-                            const uint64_t da = tc::sdesc(sa_addr + c_prod_a[pr] * kATile + ks * 256, 128, kSBO);
-                            const uint64_t db = tc::sdesc(sb_addr + c_prod_b[pr] * bpart + ks * 256, 128, kSBO);
-                            const bool first = (c == 0 && ks == 0 && pr <= 1);
-                            tc::mma_bf16(d0 + (pr ? corr : 0u), da, db, idesc, first ? 0u : 1u);
-                        }
-                    }
+                    // the issue rate of this single thread bounds the kernel: the product loop is
+                    // unrolled for the 6- and 3-product modes, and the operand descriptors are the
+                    // chunk's base descriptors plus constant offsets (start address >> 4 in bits 0-13;
+                    // shared-memory addresses stay below 2^18, so the sums do not carry)
+                    const uint64_t da0 = tc::sdesc(sa_addr, 128, kSBO), db0 = tc::sdesc(sb_addr, 128, kSBO);
+                    const uint64_t bstep = bpart >> 4;
+                    if (p.nprod == 6)
+                        mma_chunk<6>(d0, corr, da0, db0, bstep, idesc, c == 0);
+                    else if (p.nprod == 3)
+                        mma_chunk<3>(d0, corr, da0, db0, bstep, idesc, c == 0);
+                    else
+                        mma_chunk<1>(d0, corr, da0, db0, bstep, idesc, c == 0);
                     tc::mma_commit(&a_empty[sa]);
                     tc::mma_commit(&b_empty[sb]);
+                    if (++sb == nbs) {
+                        sb = 0;
+                        bph ^= 1;
+                    }
                 }
                 if (!ok) {
                     s_abort = 1;

@@ -133,6 +133,29 @@ def test_split_bw1024_forward_inverse_vs_fp64(nb):
     assert e_f <= 2e-6 and e_i <= 2e-6, (e_f, e_i)
 
 
+def test_split_repeated_runs_are_bit_identical():
+    """40 forward and 40 inverse runs at bw 256 give identical bits: the pipelines have no ordering
+    race (an unordered reuse of a staging buffer shows up as run-to-run differences in a few rows)."""
+    torch = _torch()
+    bw, nb = 256, 64
+    rng = np.random.default_rng(40)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    c_r, c_i = torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda()
+    g0 = torch.empty(nb, 4 * bw * bw, dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(c_r, c_i, g0, nb, api.PREC_BF16X3)
+    f0r, f0i = torch.empty_like(c_r), torch.empty_like(c_i)
+    plan.fst_real_f32(g0, f0r, f0i, nb, api.PREC_BF16X3)
+    g, fr, fi = torch.empty_like(g0), torch.empty_like(f0r), torch.empty_like(f0i)
+    bad = 0
+    for _ in range(40):
+        plan.inv_fst_real_f32(c_r, c_i, g, nb, api.PREC_BF16X3)
+        plan.fst_real_f32(g0, fr, fi, nb, api.PREC_BF16X3)
+        bad += int(not torch.equal(g, g0)) + int(not (torch.equal(fr, f0r) and torch.equal(fi, f0i)))
+    plan.sync_status()
+    assert bad == 0, bad
+
+
 def test_split_host_api_matches_device_api():
     torch = _torch()
     bw, nb = 64, 150  # several pipeline chunks
