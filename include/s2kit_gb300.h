@@ -169,7 +169,8 @@ typedef struct s2g_plan_s* s2g_plan;
 /* Creates a plan for bandwidth bw (2 <= bw <= 2048 for powers of two, any bw <= 512 otherwise) and a
  * seminaive/naive cutoff (1 <= cutoff <= bw).  Tables are generated on the current device
  * (FP64 recurrence and DCT, cospml.c:161-242) and shared by every plan with the same
- * (device, bw, cutoff). */
+ * (device, bw, cutoff).  A plan owns scratch buffers and streams: use it from one host thread at
+ * a time (one plan per thread for concurrent callers; the tables stay shared). */
 int s2g_plan_create(s2g_plan* plan, int bw, int cutoff);
 int s2g_plan_destroy(s2g_plan plan);
 /* Device bytes of scratch a call with this batch needs (the plan grows its own scratch
