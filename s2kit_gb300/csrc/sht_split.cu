@@ -899,6 +899,9 @@ struct Leg {
     int* err;
     int tma;                  // 1: tensor-map TMA path (below)
     uint32_t a_chunk_bytes;   // TMA bytes of one A chunk
+    int pair;                 // forward: items come in parity pairs; the odd item writes both (see k_leg_ws)
+    uint32_t stash_off;       // forward pairs: shared-memory offset of the even parity's results
+    int stash_stride;         // ... and their row stride in floats (odd)
     CUtensorMap tmA0, tmA1;   // forward: C, folded X; inverse: rc, ic
     CUtensorMap tmO;          // inverse: Fc
 };
@@ -1083,6 +1086,27 @@ __device__ __forceinline__ void epi_store(const LegClass& K, int m, int t, int n
             float* dst = K.F + (((size_t)part * K.N + f) * B + m) * (2 * B) + t * B + nb * NP + c0;
             for (int i = lane; i < w; i += 32) dst[i] = src[i];
         }
+    }
+}
+
+// Forward stores of one interleaved block of a parity pair: row r of `ep` (stride ES) holds the
+// coefficients l = m + 2 i0 + u, u < 32 (both parities), of function f0 + r % 64, part r / 64;
+// a warp writes a row's run as one contiguous store (and its mirror at order -m).
+__device__ __forceinline__ void epi_store_pair(const LegClass& K, int m, int f0, int i0, const float* ep, int ES,
+                                               int wid, int nw, int lane) {
+    const int B = K.B;
+    const int nl = min(32, B - m - 2 * i0);
+    if (lane >= nl) return;
+    const int base = index_of_harmonic_coeff(m, m, B) + 2 * i0 + lane;
+    const int nbase = index_of_harmonic_coeff(-m, m, B) + 2 * i0 + lane;
+    const float sgn = (m & 1) ? -1.f : 1.f;
+    for (int r = wid; r < 128; r += nw) {
+        const int f = f0 + (r & 63), part = r >> 6;
+        if (f >= K.N) continue;
+        const float v = ep[r * ES + lane];
+        float* out = (part ? K.ic : K.rc) + coef_base(K, f);
+        out[base] = v;
+        if (m) out[nbase] = (part ? -sgn : sgn) * v;
     }
 }
 
@@ -1652,13 +1676,23 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             uint32_t bc = 0;  // table chunks issued
             int bs = 0;       // stage of chunk bc (running: no division per chunk)
             uint32_t bph = 0; // its phase parity
+            WsItem odd{};     // parity pairs: the odd item of the pair fetched at the last even k
             for (int k = 0; !s_abort; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_empty[slot], ((k / kNI) & 1) ^ 1)) {
                     s_abort = 1;
                     break;
                 }
-                const WsItem e = decode_item<FWD>(p, atomicAdd(p.counter, 1));
+                WsItem e;
+                if (p.pair && (k & 1)) {
+                    e = odd;
+                } else {
+                    // item tables list the parities of an (order, block) next to each other and every
+                    // class holds an even number of items, so an even index starts a pair
+                    const long long idx = atomicAdd(p.counter, p.pair ? 2 : 1);
+                    e = decode_item<FWD>(p, idx);
+                    if (p.pair) odd = decode_item<FWD>(p, idx + 1);
+                }
                 items[slot] = e;
                 tc::mbar_arrive(&item_full[slot]);
                 if (e.ci < 0) break;
@@ -1811,6 +1845,50 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             const float rs = F16 ? s_rinv[slot][et] * K.tab_inv : 1.f;
             tc::tc_fence_after();
             const uint32_t trow = tmem + buf * accw + ((uint32_t)((warp & 3) * 32) << 16);
+            if (FWD && p.pair) {
+                // parity pairs: the even item (k even) parks its results in the stash and frees its
+                // accumulator at once; the odd item interleaves both parities in l and stores whole runs
+                float* stash = reinterpret_cast<float*>(smem + p.stash_off);
+                const int SST = p.stash_stride;
+                if (t != (k & 1)) {  // not a pair in order (never expected): abort, reported as a device error
+                    s_abort = 1;
+                    tc::tc_fence_before();
+                    tc::mbar_arrive(&acc_empty[buf]);
+                    tc::mbar_arrive(&item_empty[slot]);
+                    break;
+                }
+                if (t == 0) {
+                    for (int cb = 0; cb < rows; cb += 16) {
+                        float v[16];
+                        ld_sum(trow + cb, corr, p.nprod > 1, v);
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) stash[et * SST + cb + q] = v[q] * rs;
+                    }
+                    tc::tc_fence_before();
+                    tc::mbar_arrive(&acc_empty[buf]);
+                    tc::mbar_arrive(&item_empty[slot]);
+                    continue;
+                }
+                constexpr int PS = 33;  // interleave tile: 32 values of l per row, odd stride
+                for (int cb0 = 0; cb0 < rows; cb0 += 16) {
+                    float v[16];
+                    ld_sum(trow + cb0, corr, p.nprod > 1, v);
+                    if (cb0 + 16 >= rows) {  // last TMEM read of this item: release the buffer
+                        tc::tc_fence_before();
+                        tc::mbar_arrive(&acc_empty[buf]);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        ep[et * PS + 2 * q] = stash[et * SST + cb0 + q];
+                        ep[et * PS + 2 * q + 1] = v[q] * rs;
+                    }
+                    tc::named_bar_sync(1, kEpi);
+                    epi_store_pair(K, m, e.f0, n0 + cb0, ep, PS, warp - 4, 4, lane);
+                    tc::named_bar_sync(1, kEpi);
+                }
+                tc::mbar_arrive(&item_empty[slot]);
+                continue;
+            }
             if (!FWD && p.tma && !naive_order(m)) {
                 // 32-column blocks: TMEM -> 128-byte swizzled staging (two buffers) -> one TMA store
                 const float sc_ = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
@@ -2001,7 +2079,7 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     const size_t b_stage = (size_t)nt * nbmax * kKC * 2;
     // epilogue staging: the padded tile of the plain stores (and, on the tensor-map path of the
     // inverse, two 16 KB swizzled TMA-store buffers in the same place), 1024-byte multiple
-    const size_t epi = ((size_t)128 * (kEpiCols + 1) * sizeof(float) + 1023) & ~(size_t)1023;
+    size_t epi = ((size_t)128 * (kEpiCols + 1) * sizeof(float) + 1023) & ~(size_t)1023;
     int dev = 0, optin = 0, nsm = 0;
     S2G_CUDA(cudaGetDevice(&dev));
     S2G_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -2012,6 +2090,21 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     // A staging: tensor-map path, one TMA box per stage (1024-byte multiple: swizzled boxes);
     // cp.async path, per-thread slots.  As many stages as leave room for two table stages.
     const size_t stg_stride = p.tma ? ((size_t)p.a_chunk_bytes + 1023) & ~(size_t)1023 : kStgBytes;
+    // forward parity pairs (whole sectors in the coefficient stores): the even parity's results
+    // wait in a stash of 128 rows x (nbmax + 1) floats and the interleave tile is 128 x 33; taken
+    // when that still leaves two table stages and four A staging stages (at bw 256 the stash would
+    // cut the staging to two, and the shallower A prefetch costs more than the whole sectors gain)
+    p.pair = 0;
+    if (fwd && nbmax <= 128) {
+        const size_t stash = ((size_t)128 * (nbmax + 1) * sizeof(float) + 1023) & ~(size_t)1023;
+        const size_t tile = ((size_t)128 * 33 * sizeof(float) + 1023) & ~(size_t)1023;
+        const long long need = (long long)(a_bytes + (f16 ? 0 : 4 * stg_stride) + 2 * b_stage + tile + stash);
+        if (need <= budget) {
+            p.pair = 1;
+            p.stash_stride = nbmax + 1;
+            epi = tile + stash;  // the stash follows the tile inside the epilogue area
+        }
+    }
     int nstg = f16 ? 0 : kMaxStg;
     const int nstg_min = p.tma ? 1 : 2;
     long long nbs_fit = 0;
@@ -2030,6 +2123,7 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     S2G_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
     const uint32_t stg_off = (uint32_t)a_bytes, b_off = (uint32_t)(a_bytes + stg_bytes),
                    epi_off = (uint32_t)(a_bytes + stg_bytes + nbs * b_stage);
+    if (p.pair) p.stash_off = epi_off + (uint32_t)(((size_t)128 * 33 * sizeof(float) + 1023) & ~(size_t)1023);
     const uint32_t bs = (uint32_t)b_stage, ss = (uint32_t)stg_stride;
     {
         ProfScope ps_(fwd ? "leg_tc_fwd" : "leg_tc_inv", st);
