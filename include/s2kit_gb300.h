@@ -325,6 +325,13 @@ int s2g_selftest_tc(int N, int K, int nprod, const float* A, const float* B, flo
  * chunk (two CTAs per SM).  All do the same arithmetic per work item and give identical results. */
 int s2g_set_contraction_kernel(int which);
 
+/* Test hook for the failure path of the tensor-core contraction (off by default): with on != 0,
+ * the warp-specialised contraction's scheduler publishes no work, so every other role's bounded
+ * wait runs out (about half a second); the kernel then records S2G_ERR_TIMEOUT in the plan's
+ * device word, frees its tensor memory and returns.  No fault, trap or hang is involved, and the
+ * context stays usable: s2g_plan_sync_status reports the timeout and clears it. */
+int s2g_test_stall_contraction(int on);
+
 /* Kernel timing: while enabled, every kernel the library launches is bracketed by CUDA
  * events on the stream it is launched on.  s2g_prof_enable() also discards earlier records.
  * s2g_prof_report() waits for the recorded events and writes a JSON object

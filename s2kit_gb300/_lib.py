@@ -87,6 +87,7 @@ SIGNATURES = {
     "s2g_group_describe": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
     "s2g_group_sync_status": (C.c_int, [vp]),
     "s2g_set_contraction_kernel": (C.c_int, [C.c_int]),
+    "s2g_test_stall_contraction": (C.c_int, [C.c_int]),
     "s2g_tables_save": (C.c_int, [C.c_int, C.c_int, C.c_char_p]),
     "s2g_tables_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "s2g_selftest_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, vp]),

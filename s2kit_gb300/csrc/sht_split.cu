@@ -900,6 +900,7 @@ struct Leg {
     int tma;                  // 1: tensor-map TMA path (below)
     uint32_t a_chunk_bytes;   // TMA bytes of one A chunk
     int pair;                 // forward: items come in parity pairs; the odd item writes both (see k_leg_ws)
+    int stall;                // test hook: the scheduler publishes no work (every other wait runs out)
     uint32_t stash_off;       // forward pairs: shared-memory offset of the even parity's results
     int stash_stride;         // ... and their row stride in floats (odd)
     CUtensorMap tmA0, tmA1;   // forward: C, folded X; inverse: rc, ic
@@ -1677,7 +1678,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             int bs = 0;       // stage of chunk bc (running: no division per chunk)
             uint32_t bph = 0; // its phase parity
             WsItem odd{};     // parity pairs: the odd item of the pair fetched at the last even k
-            for (int k = 0; !s_abort; ++k) {
+            for (int k = 0; !s_abort && !p.stall; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_empty[slot], ((k / kNI) & 1) ^ 1)) {
                     s_abort = 1;
@@ -2066,6 +2067,7 @@ static int leg_occupancy(const void* fn, size_t smem, int* occ) {
 // Contraction kernel: 0 = k_leg_tc (all threads load, split and stage each chunk; two CTAs
 // per SM), 1 = k_leg_ws (warp-specialised, one CTA per SM).
 static std::atomic<int> g_leg_kernel{1};
+static std::atomic<int> g_leg_stall{0};  // test hook, see s2g_test_stall_contraction
 
 static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items, int* counter, cudaStream_t st) {
     const void* fn = fwd ? (f16 ? (const void*)k_leg_ws<true, true> : (const void*)k_leg_ws<true, false>)
@@ -2233,6 +2235,7 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     p.ncls = ncls;
     p.nprod = nprod;
     p.counter = counter;
+    p.stall = g_leg_stall.load();
     long long items = 0;
     int nbmax = 16;
     // tensor-map TMA path: one class, BF16 terms, contiguous batches, bw >= 64, warp-specialised kernel
@@ -2706,6 +2709,11 @@ __global__ void __launch_bounds__(128, 1) k_tc_selftest(int N, int K, int nprod,
 }
 
 }  // namespace s2g
+
+extern "C" int s2g_test_stall_contraction(int on) {
+    s2g::g_leg_stall = on ? 1 : 0;
+    return S2G_OK;
+}
 
 extern "C" int s2g_set_contraction_kernel(int which) {
     if (which < 0 || which > 2) return s2g::fail(S2G_ERR_ARG, "contraction kernel %d (0, 1 or 2)", which);

@@ -156,6 +156,36 @@ def test_split_repeated_runs_are_bit_identical():
     assert bad == 0, bad
 
 
+def test_contraction_wait_timeout_is_reported_and_recoverable():
+    """The failure path without a fault: with the test hook on, the contraction's scheduler publishes
+    no work, every other role's bounded wait runs out (about half a second), the kernel records
+    S2G_ERR_TIMEOUT and returns.  The status reaches the host, and the next transform is correct."""
+    import s2kit_gb300 as s2
+    torch = _torch()
+    lib = s2.load()
+    bw, nb = 64, 2
+    rng = np.random.default_rng(77)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    grid64, frc64, fic64 = _fp64_pair(plan, rc, ic)
+    g32 = grid64.float()
+    s_rc = torch.zeros(nb, bw * bw, dtype=torch.float32, device="cuda")
+    s_ic = torch.zeros_like(s_rc)
+    assert lib.s2g_test_stall_contraction(1) == 0
+    try:
+        plan.fst_real_f32(g32, s_rc, s_ic, nb, api.PREC_BF16X3)  # queued: returns at once
+        status = lib.s2g_plan_sync_status(plan.h)
+    finally:
+        lib.s2g_test_stall_contraction(0)
+    assert status == 5, status  # S2G_ERR_TIMEOUT, read and cleared
+    assert lib.s2g_plan_sync_status(plan.h) == 0
+    plan.fst_real_f32(g32, s_rc, s_ic, nb, api.PREC_BF16X3)
+    plan.sync_status()
+    mag = torch.hypot(frc64, fic64).amax(dim=1)
+    e = (torch.hypot(s_rc.double() - frc64, s_ic.double() - fic64).amax(dim=1) / mag).max().item()
+    assert e <= 1e-6, e
+
+
 def test_split_host_api_matches_device_api():
     torch = _torch()
     bw, nb = 64, 150  # several pipeline chunks
