@@ -404,9 +404,9 @@ def main():
     d2h = h_grid.nbytes + h_orc.nbytes + h_oic.nbytes
     # ---- grouped uneven-bandwidth workload (one graph per step), reported beside the headline
     grp = group_bench(api, torch, stream, args.steps, args.warmup, args.seed) if args.group else None
-    # ---- BASELINE configs 3 and 5, timed beside the headline
-    cfg3 = config3_bench(api, torch, stream, args.seed) if args.group else None
-    cfg5 = config5_bench(api, torch, stream, args.seed) if args.group else None
+    # ---- 4096 functions at bw 64 and 16 functions at bw 1024, timed beside the headline
+    uni64 = uniform_bw64_bench(api, torch, stream, args.seed) if args.group else None
+    big1024 = large_bw1024_bench(api, torch, stream, args.seed) if args.group else None
     cplx = complex_bench(api, torch, stream, args.seed) if args.group else None
     clk = clocks.stop()
 
@@ -445,8 +445,8 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
             "group": grp,
-            "config3": cfg3,
-            "config5": cfg5,
+            "uniform_bw64_x4096": uni64,
+            "large_bw1024_x16": big1024,
             "complex": cplx,
         }
         print(json.dumps(line), flush=True)
@@ -466,8 +466,8 @@ def _time(torch, stream, fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def config3_bench(api, torch, stream, seed):
-    """BASELINE config 3: 4096 real functions at bw 64, FP32 grids, coefficients N(0,1)(1+l)^-1.5,
+def uniform_bw64_bench(api, torch, stream, seed):
+    """4096 real functions at bw 64, FP32 grids, coefficients N(0,1)(1+l)^-1.5,
     split BF16X3 fwd+inv; error of the split forward against the FP64 path on the same grid."""
     B, N = 64, 4096
     rc, ic = real_field_coeffs(np.random.default_rng(seed + 3), B, 1.5, N)
@@ -531,8 +531,8 @@ def complex_bench(api, torch, stream, seed):
             "unit": "fwd+inv functions/s", "ms_per_step": ms, "coeff_err_vs_fp64": err}
 
 
-def config5_bench(api, torch, stream, seed):
-    """BASELINE config 5: 16 real functions at bw 1024, (1+l)^-1: split BF16X3 fwd+inv, the FP64-residual
+def large_bw1024_bench(api, torch, stream, seed):
+    """16 real functions at bw 1024, (1+l)^-1: split BF16X3 fwd+inv, the FP64-residual
     refined forward and the FP64 fwd+inv, with the errors against the FP64 path."""
     B, N = 1024, 16
     rc, ic = real_field_coeffs(np.random.default_rng(seed + 5), B, 1.0, N)

@@ -79,7 +79,7 @@ def main():
 
     # ---- reference outputs on seeded inputs ----------------------------------------
     rng = np.random.default_rng(20240601)
-    # round trips through the reference API (BASELINE config 1 uses B=64, p=0)
+    # round trips through the reference API (the single-function workload uses B=64, p=0)
     cases = [(8, 8, COMPLEX, 0.0), (16, 4, COMPLEX, 0.0), (32, 32, REAL, 1.0), (64, 64, REAL, 0.0),
              (64, 16, COMPLEX, 1.0)]
     for bw, cut, fmt, p in cases:

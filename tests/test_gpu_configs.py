@@ -1,4 +1,4 @@
-"""BASELINE configurations 3 and 5 on the GPU (configs 1 and 2 are in test_gpu_fp64.py).
+"""The batched uniform workload (4096 functions at bw 64) and the large one (bw 1024) on the GPU.
 
 Config 3: 4096 real functions at bw 64 in one launch, FP32 samples, coefficients
 N(0,1)(1+l)^-1.5, 3-term split BF16 contraction: error vs the FP64 path <= 1e-6 (normwise).
@@ -16,7 +16,7 @@ from tests._util import harmonic_index, real_field_coeffs
 pytestmark = pytest.mark.gpu
 
 
-def test_config3_batched_uniform_bw64():
+def test_batched_uniform_4096_functions_bw64():
     import torch
     bw, nb = 64, 4096
     rng = np.random.default_rng(3)
@@ -39,7 +39,7 @@ def test_config3_batched_uniform_bw64():
     assert e_fwd <= 1e-6 and e_inv <= 1e-6, (e_fwd, e_inv)
 
 
-def test_config5_fp64_bw1024_roundtrip_and_conv():
+def test_bw1024_fp64_roundtrip_and_conv():
     import torch
     bw, nb = 1024, 2
     rng = np.random.default_rng(5)
@@ -80,7 +80,7 @@ def test_config5_fp64_bw1024_roundtrip_and_conv():
 
 
 @pytest.mark.parametrize("prec", [api.PREC_BF16X3])
-def test_config5_split_bw1024_with_fp64_residual_refinement(prec):
+def test_bw1024_split_with_fp64_residual_refinement(prec):
     """16 real functions at bw 1024: the split path alone, then with one FP64-residual refinement
     step (forward and inverse) to <= 1e-10 against the FP64 path."""
     import torch

@@ -2,8 +2,8 @@
 
 Tolerances: the reference's own FP64 results are the target; FFT/DCT implementations and
 FMA contraction differ, so results agree to rounding.  Normwise relative error
-max|gpu - ref| / max|ref| <= 1e-11 is the parity bar (BASELINE: plain FP64 GPU path
-within 1e-11 relative of the reference).
+max|gpu - ref| / max|ref| <= 1e-11 is the parity bar (the plain FP64 GPU path within 1e-11
+relative of the reference).
 """
 import numpy as np
 import pytest
@@ -208,7 +208,7 @@ def test_dropin_vs_oracle(oracle, bw, cut, fmt):
     assert np.abs(gr - orr).max() <= TOL * s and np.abs(gi - ori).max() <= TOL * s
 
 
-def test_config1_roundtrip_bw64():
+def test_single_function_roundtrip_bw64():
     """B=64 real field, N(0,1) coefficients with conjugate symmetry: InvFST then FST <= 1e-11."""
     rng = np.random.default_rng(2024)
     rc, ic = real_field_coeffs(rng, 64, 0.0)
@@ -284,7 +284,7 @@ def test_batched_complex_and_conv(oracle):
         assert np.abs(cr[f].cpu().numpy() - occ).max() <= TOL * np.abs(occ).max()
 
 
-def test_config2_bw256_fwd_inv_conv(oracle):
+def test_single_function_bw256_fwd_inv_conv(oracle):
     """B=256 real field, coefficients N(0,1)(1+l)^-1; forward+inverse and the zonal-filter
     convolution h_l^0 = exp(-l(l+1)/(2*40^2)) against the oracle."""
     torch = _torch()

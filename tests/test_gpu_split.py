@@ -2,7 +2,7 @@
 
 Error metric: normwise relative error max|x - x_ref| / max|x_ref| per function (coefficients
 for the forward, samples for the inverse), reference = FP64.  Stated tolerances:
-  S2G_PREC_BF16X3 (6 split products, FP32 FFT/DCT): <= 1e-6   (BASELINE headline tolerance)
+  S2G_PREC_BF16X3 (6 split products, FP32 FFT/DCT): <= 1e-6   (the headline tolerance)
   S2G_PREC_BF16X2 (3 split products):               <= 1e-4
   S2G_PREC_FP16X2 (2-term FP16, 3 products):        <= 2e-6 for bw <= 256, <= 5e-6 at bw 512
     (two FP16 terms hold 22 bits: about 2^-22 per product before cancellation in the sums)

@@ -110,7 +110,7 @@ def test_odd_bandwidth_roundtrip(oracle, bw):
     assert rel_err_norm(fr, fi, rc, ic) <= 1e-12
 
 
-def test_baseline_config1_roundtrip(oracle):
+def test_single_function_bw64_roundtrip(oracle):
     """B=64 real field, coefficients N(0,1) with conjugate symmetry, round trip <= 1e-11."""
     rng = np.random.default_rng(1)
     rc, ic = real_field_coeffs(rng, 64, 0.0)
