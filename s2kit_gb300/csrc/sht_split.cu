@@ -437,7 +437,10 @@ struct FftSmem {
     static constexpr int PSA = (((S + S / 32) + 31) & ~31) + 4;
     static constexpr int RS = B + B / 32 + 1;                    // padded transpose row (odd)
     static constexpr int TILE = (FftShape<R>::LAT * RS + 3) & ~3; // one plane of the row kernels' tile
-    static constexpr int TS = FftShape<R>::LAT + 1;              // rows-inverse tile row (odd)
+    // rows-inverse tile, latitude-major [LAT][TS] per plane: TS = B + 2 (2 mod 32 for B >= 32, 18 at
+    // B = 16) spreads a warp's float4-component stores (8 orders x 4 latitude groups) over 32 banks,
+    // and the per-warp gathers of one latitude over consecutive orders are conflict-free
+    static constexpr int TS = B + 2;
     // the four-step warp FFT exchanges through the warp's spectrum rows
     static_assert((R != 8 && R != 16 && R != 32) || R * (32 + 32 / R) <= PSA, "exchange planes fit the spectrum rows");
     // R = 64 (WarpFFT2048): the odd pass exchanges in [OFF, OFF + 32 * 33), the spectrum reaches pad32(2047)
@@ -741,13 +744,13 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
     using L = FftSmem<R>;
     constexpr int S = L::S, B = L::B, PSA = L::PSA, TS = L::TS;
     constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
-    static_assert(S % LAT == 0 && LAT % 4 == 0 && (B * TS) % 4 == 0, "row staging");
+    static_assert(S % LAT == 0 && LAT % 4 == 0, "row staging");
     extern __shared__ __align__(16) float fsm[];
-    // the order-major tile [B][TS] (re, im) is dead once every warp holds its inputs; the warps'
+    // the latitude-major tile [LAT][TS] (re, im) is dead once every warp holds its inputs; the warps'
     // spectrum buffers [W][PSA] (re, im) then reuse the same space
-    constexpr int U = 2 * B * TS > 2 * W * PSA ? 2 * B * TS : 2 * W * PSA;
+    constexpr int U = 2 * LAT * TS > 2 * W * PSA ? 2 * LAT * TS : 2 * W * PSA;
     float* tr = fsm;
-    float* ti = tr + B * TS;
+    float* ti = tr + LAT * TS;
     float* spr = fsm;
     float* spi = spr + W * PSA;
     float2* tw = reinterpret_cast<float2*>(fsm + U);
@@ -783,10 +786,10 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
             const int e = threadIdx.x + (it0 + u) * T;
             if (e < B * Q4) {
                 const int m = e / Q4, q = 4 * (e - m * Q4);
-                float* pr = tr + m * TS + q;
-                float* pi = ti + m * TS + q;
-                pr[0] = a[u].x, pr[1] = a[u].y, pr[2] = a[u].z, pr[3] = a[u].w;
-                pi[0] = b[u].x, pi[1] = b[u].y, pi[2] = b[u].z, pi[3] = b[u].w;
+                float* pr = tr + q * TS + m;
+                float* pi = ti + q * TS + m;
+                pr[0] = a[u].x, pr[TS] = a[u].y, pr[2 * TS] = a[u].z, pr[3 * TS] = a[u].w;
+                pi[0] = b[u].x, pi[TS] = b[u].y, pi[2 * TS] = b[u].z, pi[3 * TS] = b[u].w;
             }
         }
     }
@@ -795,16 +798,16 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
     auto in = [&](int m) {
         float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
         if (m < B) {
-            ar = tr[m * TS + a];
-            ai = (m == 0) ? 0.f : ti[m * TS + a];
-            br = tr[m * TS + b];
-            bi = (m == 0) ? 0.f : ti[m * TS + b];
+            ar = tr[a * TS + m];
+            ai = (m == 0) ? 0.f : ti[a * TS + m];
+            br = tr[b * TS + m];
+            bi = (m == 0) ? 0.f : ti[b * TS + m];
         } else if (m > B) {
             const int mm = S - m;
-            ar = tr[mm * TS + a];
-            ai = -ti[mm * TS + a];
-            br = tr[mm * TS + b];
-            bi = -ti[mm * TS + b];
+            ar = tr[a * TS + mm];
+            ai = -ti[a * TS + mm];
+            br = tr[b * TS + mm];
+            bi = -ti[b * TS + mm];
         }
         return make_float2(ar - bi, ai + br);  // F_a + i F_b
     };
@@ -2364,7 +2367,7 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
         k_dct_inv_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, nrows,
                                                                         s->sin32, s->twS, s->twD, scale);
     } else {  // rows inverse
-        smem = std::max(sizeof(float) * 2 * B * L::TS, spec) + tw_bytes;
+        smem = std::max(sizeof(float) * 2 * kLatPerCta * L::TS, spec) + tw_bytes;
         S2G_TRY(set_smem((const void*)k_rows_inv_w<R>, smem));
         const int g = N * (S / kLatPerCta);  // one tile per CTA: fresh CTAs overlap loads better than a loop
         ProfScope ps_("rows_inv_f32", st);
