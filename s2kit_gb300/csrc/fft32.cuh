@@ -192,6 +192,28 @@ struct WarpFFT {
 // 32 lanes hold 32 consecutive indices, so spectrum stores through pad32 are conflict-free.
 // Shared-memory traffic per transform: R exchange writes and reads per plane and log2(P) R
 // shuffles, against 10 R shuffles of the lane-butterfly form.
+// u[K] *= w_32^(h K), K = K0 .. R-1, for a runtime h in 1 .. P-1 (P <= 4): the P-1 candidate
+// factors of each K are compile-time constants and h selects one.
+template <int R, int P, int K>
+struct C3Const {
+    __device__ __forceinline__ static void run(float2* u, int h, float sign) {
+        constexpr float c1 = ct::cosf_(K % 32, 32), s1 = ct::sinf_(K % 32, 32);
+        constexpr float c2 = ct::cosf_((2 * K) % 32, 32), s2 = ct::sinf_((2 * K) % 32, 32);
+        constexpr float c3 = ct::cosf_((3 * K) % 32, 32), s3 = ct::sinf_((3 * K) % 32, 32);
+        float c = c1, s = s1;
+        if (P > 2) {
+            c = h == 1 ? c1 : (h == 2 ? c2 : c3);
+            s = h == 1 ? s1 : (h == 2 ? s2 : s3);
+        }
+        u[K] = cmulf(u[K], make_float2(c, sign * s));
+        C3Const<R, P, K + 1>::run(u, h, sign);
+    }
+};
+template <int R, int P>
+struct C3Const<R, P, R> {
+    __device__ __forceinline__ static void run(float2*, int, float) {}
+};
+
 template <int R>
 struct WarpFFT4 {
     static_assert(R == 8 || R == 16 || R == 32, "four-step warp FFT: R = 8, 16 or 32");
@@ -265,13 +287,19 @@ struct WarpFFT4 {
         __syncwarp();  // the exchange planes are free again (callers reuse them)
         RegStages<R, 2>::run(u, sign);
         if constexpr (P > 1) {
-            // (c3) T_h[k] = w_32^(h k) Y_h[k], then the P-point DFT across the column's lanes
+            // (c3) T_h[k] = w_32^(h k) Y_h[k], then the P-point DFT across the column's lanes.  For
+            // P <= 4 the factors are compile-time constants (h = 1..P-1 picks one per k); no
+            // shared-memory table read.
             if (h) {
+                if constexpr (P <= 4) {
+                    C3Const<R, P, 1>::run(u, h, sign);
+                } else {
 #pragma unroll
-                for (int k = 1; k < R; ++k) {
-                    float2 w = tw[padtw(((h * k) & 31) * R)];
-                    w.y *= sign;
-                    u[k] = cmulf(u[k], w);
+                    for (int k = 1; k < R; ++k) {
+                        float2 w = tw[padtw(((h * k) & 31) * R)];
+                        w.y *= sign;
+                        u[k] = cmulf(u[k], w);
+                    }
                 }
             }
             stage<0>(u, tw, h, sign);
