@@ -18,11 +18,10 @@ namespace s2g {
 // Output X[f][m][theta] for m < rows_out, scaled.
 template <typename T, typename T2>
 __global__ void k_rows_fwd(const T* __restrict__ rdata, const T* __restrict__ idata,
-                           T* __restrict__ Xr, T* __restrict__ Xi, int S, int logS, int rows_out, int R,
+                           T* __restrict__ Xr, T* __restrict__ Xi, int S, const Len L, int rows_out, int R,
                            T scale, const T2* __restrict__ tw) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     T* sm = reinterpret_cast<T*>(sm_raw);
-    const Len L{S, logS};
     const int SP = S + 1;
     T* re = sm;
     T* im = re + (size_t)R * SP;
@@ -84,11 +83,10 @@ __global__ void k_rows_fwd(const T* __restrict__ rdata, const T* __restrict__ id
 //   real output (rdata only, idata == null): two latitudes per complex DFT
 template <typename T, typename T2>
 __global__ void k_rows_inv(const T* __restrict__ Fr, const T* __restrict__ Fi, int frows, int fmt_complex,
-                           T* __restrict__ rdata, T* __restrict__ idata, int S, int logS, int R,
+                           T* __restrict__ rdata, T* __restrict__ idata, int S, const Len L, int R,
                            const T2* __restrict__ tw) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     T* sm = reinterpret_cast<T*>(sm_raw);
-    const Len L{S, logS};
     const int B = S / 2;
     const int SP = S + 1;
     T* re = sm;

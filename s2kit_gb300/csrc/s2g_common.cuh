@@ -20,7 +20,18 @@ namespace s2g {
 struct Len {
     int n;      // length
     int logn;   // log2(n) when n is a power of two, else -1
+    // Non power-of-two n with tables (Bluestein's chirp-z transform, see block_dft): M, a power of
+    // two >= 2n - 1, and device tables chirp[j] = exp(-i pi j^2 / n) (j < n), the spectra of the
+    // convolution kernel for sign -1 and +1 (M entries in bit-reversed order, 1/M folded in) and
+    // twM[k] = exp(2 pi i k / M) (k < M/2).  Without tables (M = 0) the DFT is direct, O(n^2).
+    int M = 0, logM = -1;
+    const double2* chirp = nullptr;
+    const double2* bfwd = nullptr;
+    const double2* binv = nullptr;
+    const double2* twM = nullptr;
     __host__ __device__ bool pow2() const { return logn >= 0; }
+    // reals of scratch block_dft needs (`tmp`)
+    __host__ __device__ int tmp_len() const { return pow2() ? 0 : (M > 0 ? 2 * M : 2 * n); }
     // position at which input element k must be stored before block_dft()
     __device__ __forceinline__ int pos(int k) const {
         return logn > 0 ? (int)(__brev((unsigned)k) >> (32 - logn)) : k;
@@ -39,7 +50,11 @@ inline Len make_len(int n) {
 // ---------------------------------------------------------------------------------
 // In-place DFT of `cnt` sequences re/im[s*stride + k], k < L.n (input in L.pos order).
 // tw[k] = (cos(2 pi k / n), sin(2 pi k / n)) for k < n.  Ends with __syncthreads().
-// For non power-of-two n, `tmp` must hold 2*n reals (used one sequence at a time).
+// For non power-of-two n, `tmp` holds L.tmp_len() reals (used one sequence at a time).  With
+// Bluestein tables the length-n DFT is a length-M cyclic convolution (Bluestein 1970):
+//   X[k] = h_k sum_j (x_j h_j) conj(h_{k-j}),  h_j = exp(sign i pi j^2 / n),
+// computed as a decimation-in-frequency FFT (natural in, bit-reversed out), a product with the
+// kernel's precomputed spectrum, and a decimation-in-time inverse FFT (bit-reversed in).
 template <typename T, typename T2>
 __device__ void block_dft(T* re, T* im, Len L, int cnt, int stride, const T2* __restrict__ tw, T sign,
                           T* tmp) {
@@ -68,6 +83,76 @@ __device__ void block_dft(T* re, T* im, Len L, int cnt, int stride, const T2* __
                 i[a1] = yi - xi;
                 r[a0] = yr + xr;
                 i[a0] = yi + xi;
+            }
+            __syncthreads();
+        }
+        return;
+    }
+    if (L.M > 0) {
+        const int M = L.M, lM = L.logM;
+        T* ar = tmp;
+        T* ai = tmp + M;
+        const double2* bf = sign < 0 ? L.bfwd : L.binv;
+        const T hs = sign < 0 ? T(1) : T(-1);  // h = chirp (sign -1) or its conjugate
+        for (int seq = 0; seq < cnt; ++seq) {
+            T* r = re + (size_t)seq * stride;
+            T* i = im + (size_t)seq * stride;
+            for (int k = threadIdx.x; k < M; k += blockDim.x) {
+                T xr = 0, xi = 0;
+                if (k < n) {
+                    const double2 h = L.chirp[k];
+                    const T hr = (T)h.x, hi = hs * (T)h.y, a = r[k], b = i[k];
+                    xr = a * hr - b * hi;
+                    xi = a * hi + b * hr;
+                }
+                ar[k] = xr;
+                ai[k] = xi;
+            }
+            __syncthreads();
+            for (int s = lM; s >= 1; --s) {  // decimation in frequency, sign -1
+                const int half = 1 << (s - 1);
+                for (int t = threadIdx.x; t < M / 2; t += blockDim.x) {
+                    const int j = t & (half - 1);
+                    const int a0 = ((t >> (s - 1)) << s) + j, a1 = a0 + half;
+                    const double2 w = L.twM[j << (lM - s)];
+                    const T c = (T)w.x, sn = -(T)w.y;
+                    const T ur = ar[a0], ui = ai[a0], vr = ar[a1], vi = ai[a1];
+                    ar[a0] = ur + vr;
+                    ai[a0] = ui + vi;
+                    const T dr = ur - vr, di = ui - vi;
+                    ar[a1] = dr * c - di * sn;
+                    ai[a1] = dr * sn + di * c;
+                }
+                __syncthreads();
+            }
+            for (int k = threadIdx.x; k < M; k += blockDim.x) {  // times the kernel's spectrum
+                const double2 b = bf[k];
+                const T xr = ar[k], xi = ai[k];
+                ar[k] = xr * (T)b.x - xi * (T)b.y;
+                ai[k] = xr * (T)b.y + xi * (T)b.x;
+            }
+            __syncthreads();
+            for (int s = 1; s <= lM; ++s) {  // decimation in time, sign +1
+                const int half = 1 << (s - 1);
+                for (int t = threadIdx.x; t < M / 2; t += blockDim.x) {
+                    const int j = t & (half - 1);
+                    const int a0 = ((t >> (s - 1)) << s) + j, a1 = a0 + half;
+                    const double2 w = L.twM[j << (lM - s)];
+                    const T c = (T)w.x, sn = (T)w.y;
+                    const T xr = ar[a1] * c - ai[a1] * sn, xi = ar[a1] * sn + ai[a1] * c;
+                    const T yr = ar[a0], yi = ai[a0];
+                    ar[a1] = yr - xr;
+                    ai[a1] = yi - xi;
+                    ar[a0] = yr + xr;
+                    ai[a0] = yi + xi;
+                }
+                __syncthreads();
+            }
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
+                const double2 h = L.chirp[k];
+                const T hr = (T)h.x, hi = hs * (T)h.y, cr = ar[k], ci = ai[k];
+                r[k] = cr * hr - ci * hi;
+                i[k] = cr * hi + ci * hr;
             }
             __syncthreads();
         }

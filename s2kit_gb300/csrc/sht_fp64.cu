@@ -17,6 +17,10 @@
 // The real-field fast path (no imaginary samples) packs two latitudes into one complex DFT.
 #include <math.h>
 
+#include <map>
+#include <mutex>
+#include <vector>
+
 #include "rows.cuh"
 #include "s2g_common.cuh"
 #include "s2g_internal.h"
@@ -69,7 +73,8 @@ struct FwdDlt {
     const double* w;
     const double2* twS;
     const double2* twD;
-    int B, S, logS, cutoff, nfunc, G;
+    int B, S, cutoff, nfunc, G;
+    Len L;                 // DFT length S (with Bluestein tables when S is not a power of two)
     int complex_rows;      // rows 0..B-1 and B+1..S-1 (COMPLEX) else 0..B-1
     int real_mirror;       // fill f(l,-m) = (-1)^m conj f(l,m)
     int one_d, m1d;        // single order from row 0 of X, output contiguous result[l-m]
@@ -78,7 +83,7 @@ struct FwdDlt {
 __global__ void k_fwd_dlt(FwdDlt p) {
     extern __shared__ double sm[];
     const int B = p.B, S = p.S;
-    const Len L{S, p.logS};
+    const Len L = p.L;
     const int Ge = (p.G + 1) & ~1;
     int row, m;
     bool neg = false;
@@ -98,7 +103,7 @@ __global__ void k_fwd_dlt(FwdDlt p) {
     double* zr = sm;
     double* zi = zr + S;
     double* tmp = zi + S;
-    double* cbuf = tmp + (L.pow2() ? 0 : 2 * S);
+    double* cbuf = tmp + L.tmp_len();
     const int clen = semi ? B : S;  // per function per part
     double* cre = cbuf;                          // [Ge][clen]
     double* cim = cbuf + (size_t)Ge * clen;      // [Ge][clen]
@@ -219,7 +224,8 @@ struct InvDlt {
     const double* sinv;
     const double2* twS;
     const double2* twD;
-    int B, S, logS, cutoff, nfunc, G;
+    int B, S, cutoff, nfunc, G;
+    Len L;                 // DFT length S (with Bluestein tables when S is not a power of two)
     int complex_rows;
     int one_d, m1d;
     double out_scale;
@@ -228,7 +234,7 @@ struct InvDlt {
 __global__ void k_inv_dlt(InvDlt p) {
     extern __shared__ double sm[];
     const int B = p.B, S = p.S;
-    const Len L{S, p.logS};
+    const Len L = p.L;
     const int Ge = (p.G + 1) & ~1;
     int row, m;
     bool neg = false;
@@ -249,7 +255,7 @@ __global__ void k_inv_dlt(InvDlt p) {
     double* zr = sm;
     double* zi = zr + S;
     double* tmp = zi + S;
-    double* are = tmp + (L.pow2() ? 0 : 2 * S);  // [Ge][B]
+    double* are = tmp + L.tmp_len();              // [Ge][B]
     double* aim = are + (size_t)Ge * B;           // [Ge][B]
     double* fre = aim + (size_t)Ge * B;           // [Ge][B]  (semi only)
     double* fim = fre + (size_t)Ge * B;
@@ -417,30 +423,97 @@ static int rows_per_cta(int S) {
     return R;
 }
 
-static size_t rows_smem(int S, int R) {
-    const Len L = make_len(S);
-    return ((size_t)2 * R * (S + 1) + (L.pow2() ? 0 : 2 * S)) * sizeof(double);
+// DFT length n with, when n is not a power of two, Bluestein tables on the current device
+// (built once per device and n, host arithmetic in long double; see Len and block_dft).
+static int dft_len(int n, Len* out) {
+    Len L = make_len(n);
+    if (L.pow2() || n < 2) {
+        *out = L;
+        return S2G_OK;
+    }
+    int dev = 0;
+    S2G_CUDA(cudaGetDevice(&dev));
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, Len> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto it = cache.find({dev, n});
+    if (it != cache.end()) {
+        *out = it->second;
+        return S2G_OK;
+    }
+    int M = 1, lM = 0;
+    while (M < 2 * n - 1) M <<= 1, ++lM;
+    const long double pi = 3.141592653589793238462643383279502884L;
+    std::vector<double2> h(n), tab((size_t)n + 2 * (size_t)M + M / 2);
+    std::vector<long double> rc(M), rs(M);
+    for (int k = 0; k < M; ++k) rc[k] = cosl(2 * pi * k / M), rs[k] = sinl(2 * pi * k / M);
+    std::vector<long double> hc(n), hsn(n);  // exp(-i pi j^2 / n), angle reduced exactly: j^2 mod 2n
+    for (int j = 0; j < n; ++j) {
+        const long double a = pi * (long double)(((long long)j * j) % (2LL * n)) / n;
+        hc[j] = cosl(a), hsn[j] = -sinl(a);
+        tab[j] = make_double2((double)hc[j], (double)hsn[j]);
+    }
+    for (int sg = 0; sg < 2; ++sg) {  // sg 0: sign -1 (h = chirp), 1: sign +1 (h = conj chirp)
+        // kernel b[m] = conj(h_m) at m and M - m (|m| < n); its DFT (sign -1) / M, bit-reversed order
+        const long double bi_sign = sg == 0 ? -1.0L : 1.0L;  // imaginary part of conj(h) = -(+-hsn)
+        for (int k = 0; k < M; ++k) {
+            long double sr = 0, si = 0;
+            for (int m = -(n - 1); m <= n - 1; ++m) {
+                const int am = m < 0 ? -m : m, pm = m < 0 ? M + m : m;
+                const long double br = hc[am], bim = bi_sign * hsn[am];
+                const int idx = (int)(((long long)pm * k) % M);
+                const long double c = rc[idx], s_ = -rs[idx];
+                sr += br * c - bim * s_;
+                si += br * s_ + bim * c;
+            }
+            int rk = 0;
+            for (int b = 0; b < lM; ++b) rk |= ((k >> b) & 1) << (lM - 1 - b);
+            tab[(size_t)n + (size_t)sg * M + rk] = make_double2((double)(sr / M), (double)(si / M));
+        }
+    }
+    for (int k = 0; k < M / 2; ++k) tab[(size_t)n + 2 * (size_t)M + k] = make_double2((double)rc[k], (double)rs[k]);
+    double2* d = nullptr;
+    S2G_CUDA(cudaMalloc(&d, sizeof(double2) * tab.size()));
+    const cudaError_t e = cudaMemcpy(d, tab.data(), sizeof(double2) * tab.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "cudaMemcpy");
+    }
+    L.M = M;
+    L.logM = lM;
+    L.chirp = d;
+    L.bfwd = d + n;
+    L.binv = d + n + M;
+    L.twM = d + n + 2 * M;
+    cache[{dev, n}] = L;
+    *out = L;
+    return S2G_OK;
+}
+
+static size_t rows_smem(const Len& L, int R) {
+    return ((size_t)2 * R * (L.n + 1) + L.tmp_len()) * sizeof(double);
 }
 
 static int launch_rows_fwd(const double* rdata, const double* idata, double* Xr, double* Xi, int B, int rows_out,
                            int batch, const double2* tw, cudaStream_t st) {
     const int S = 2 * B;
-    const Len L = make_len(S);
+    Len L;
+    S2G_TRY(dft_len(S, &L));
     const int R = rows_per_cta(S);
     const int lat_per = idata ? R : 2 * R;
-    const size_t smem = rows_smem(S, R);
+    const size_t smem = rows_smem(L, R);
     S2G_TRY(set_smem((const void*)k_rows_fwd<double, double2>, smem));
     dim3 grid((S + lat_per - 1) / lat_per, batch);
     {
         ProfScope ps_("rows_fwd_f64", st);
-        k_rows_fwd<double, double2><<<grid, 256, smem, st>>>(rdata, idata, Xr, Xi, S, L.logn, rows_out, R, sqrt(2.0 * kPi) / S, tw);
+        k_rows_fwd<double, double2><<<grid, 256, smem, st>>>(rdata, idata, Xr, Xi, S, L, rows_out, R, sqrt(2.0 * kPi) / S, tw);
     }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;
 }
 
-static int pick_group(int B, int S, bool naive, bool pow2, size_t* smem_out, size_t per_g_extra = 0) {
-    const size_t fixed = ((size_t)2 * S + (pow2 ? 0 : 2 * S)) * sizeof(double);
+static int pick_group(int B, int S, bool naive, int tmp_len, size_t* smem_out, size_t per_g_extra = 0) {
+    const size_t fixed = ((size_t)2 * S + tmp_len) * sizeof(double);
     const size_t per_g = (size_t)2 * (naive ? S : B) * sizeof(double) + per_g_extra;
     const size_t budget = 160 * 1024;
     int G = 8;
@@ -451,13 +524,14 @@ static int pick_group(int B, int S, bool naive, bool pow2, size_t* smem_out, siz
 }
 
 static int launch_fwd_dlt(FwdDlt p, int nrows_grid, cudaStream_t st) {
-    const Len L = make_len(p.S);
+    Len L;
+    S2G_TRY(dft_len(p.S, &L));
     size_t smem = 0;
     const bool any_naive = p.one_d ? (p.m1d >= p.cutoff) : (p.cutoff < p.B);
-    const int G = pick_group(p.B, p.S, any_naive, L.pow2(), &smem);
+    const int G = pick_group(p.B, p.S, any_naive, L.tmp_len(), &smem);
     if (!G) return fail(S2G_ERR_UNSUPPORTED, "bandwidth %d too large for the FP64 DLT kernel", p.B);
     p.G = G;
-    p.logS = L.logn;
+    p.L = L;
     S2G_TRY(set_smem((const void*)k_fwd_dlt, smem));
     dim3 grid(nrows_grid, (p.nfunc + G - 1) / G);
     {
@@ -469,9 +543,10 @@ static int launch_fwd_dlt(FwdDlt p, int nrows_grid, cudaStream_t st) {
 }
 
 static int launch_inv_dlt(InvDlt p, int nrows_grid, cudaStream_t st) {
-    const Len L = make_len(p.S);
+    Len L;
+    S2G_TRY(dft_len(p.S, &L));
     // are, aim, fre, fim: 4*B per function; plus B+33 ints
-    const size_t fixed = ((size_t)2 * p.S + (L.pow2() ? 0 : 2 * p.S)) * sizeof(double) +
+    const size_t fixed = ((size_t)2 * p.S + L.tmp_len()) * sizeof(double) +
                          (size_t)(p.B + 1 + 32) * sizeof(int);
     const size_t per_g = (size_t)4 * p.B * sizeof(double);
     int G = 8;
@@ -479,7 +554,7 @@ static int launch_inv_dlt(InvDlt p, int nrows_grid, cudaStream_t st) {
     const size_t smem = fixed + (size_t)G * per_g;
     if (smem > 220 * 1024) return fail(S2G_ERR_UNSUPPORTED, "bandwidth %d too large for the FP64 DLT kernel", p.B);
     p.G = G;
-    p.logS = L.logn;
+    p.L = L;
     S2G_TRY(set_smem((const void*)k_inv_dlt, smem));
     dim3 grid(nrows_grid, (p.nfunc + G - 1) / G);
     {
@@ -550,15 +625,16 @@ int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rda
     p.complex_rows = (data_format == COMPLEX);
     p.out_scale = 1.0 / sqrt(2.0 * kPi);  // FST_semi_memo.c:344-348
     S2G_TRY(launch_inv_dlt(p, (data_format == COMPLEX) ? S - 1 : B, st));
-    const Len L = make_len(S);
+    Len L;
+    S2G_TRY(dft_len(S, &L));
     const int R = rows_per_cta(S);
     const int lat_per = idata ? R : 2 * R;
-    const size_t smem = rows_smem(S, R);
+    const size_t smem = rows_smem(L, R);
     S2G_TRY(set_smem((const void*)k_rows_inv<double, double2>, smem));
     dim3 grid((S + lat_per - 1) / lat_per, batch);
     {
         ProfScope ps_("rows_inv_f64", st);
-        k_rows_inv<double, double2><<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L.logn, R, t->tw_S);
+        k_rows_inv<double, double2><<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L, R, t->tw_S);
     }
     S2G_CUDA(cudaGetLastError());
     return S2G_OK;

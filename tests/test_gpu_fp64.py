@@ -325,3 +325,33 @@ def test_status_errors_on_gpu():
         plan.fst(None, None, None, None, 1)
     with pytest.raises(s2.S2GError):
         plan.fst(1, None, 1, 1, 0)  # batch 0
+
+
+@pytest.mark.parametrize("bw,fmt", [(31, api.REAL), (48, api.COMPLEX), (127, api.REAL), (255, api.COMPLEX)])
+def test_fp64_non_power_of_two_bandwidths_vs_oracle(oracle, bw, fmt):
+    """Odd and non-power-of-two bandwidths on the batched FP64 path, whose length-2bw DFTs run as
+    Bluestein convolutions (power-of-two FFTs against precomputed chirp spectra), against the
+    oracle, both directions, to the FP64 parity bar."""
+    torch = _torch()
+    nb = 2
+    rng = np.random.default_rng(bw)
+    if fmt == api.REAL:
+        rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    else:
+        rc, ic = rng.standard_normal((nb, bw * bw)), rng.standard_normal((nb, bw * bw))
+    plan = api.Plan(bw, bw)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    gr = torch.zeros(nb, 4 * bw * bw, dtype=torch.float64, device="cuda")
+    gi = torch.zeros_like(gr)
+    plan.inv_fst(d_rc, d_ic, gr, gi if fmt == api.COMPLEX else None, nb, fmt)
+    o_r, o_i = torch.zeros_like(d_rc), torch.zeros_like(d_ic)
+    plan.fst(gr, gi if fmt == api.COMPLEX else None, o_r, o_i, nb, fmt)
+    torch.cuda.synchronize()
+    for f in range(nb):
+        er, ei = oracle.inv_fst(rc[f], ic[f], bw, fmt, bw)
+        g_r = gr[f].cpu().numpy()
+        g_i = gi[f].cpu().numpy() if fmt == api.COMPLEX else np.zeros_like(g_r)
+        if fmt == api.REAL:
+            ei = np.zeros_like(er)
+        assert rel_err_norm(g_r, g_i, er, ei) <= TOL
+        assert rel_err_norm(o_r[f].cpu().numpy(), o_i[f].cpu().numpy(), rc[f], ic[f]) <= TOL
