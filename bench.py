@@ -408,6 +408,7 @@ def main():
     uni64 = uniform_bw64_bench(api, torch, stream, args.seed) if args.group else None
     big1024 = large_bw1024_bench(api, torch, stream, args.seed) if args.group else None
     cplx = complex_bench(api, torch, stream, args.seed) if args.group else None
+    odd = odd_bw_bench(api, torch, stream, args.seed) if args.group else None
     clk = clocks.stop()
 
     # ---- CPU baseline (rank 0): bounded sample of the same workload on all host cores
@@ -448,6 +449,7 @@ def main():
             "uniform_bw64_x4096": uni64,
             "large_bw1024_x16": big1024,
             "complex": cplx,
+            "odd_bw255_fp64": odd,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -495,6 +497,26 @@ def uniform_bw64_bench(api, torch, stream, seed):
     err = (torch.hypot(s_r.double() - f_r, s_i.double() - f_i).amax(dim=1) / mag).max().item()
     return {"workload": "4096 real functions at bw 64, (1+l)^-1.5, split BF16X3, fwd+inv", "value": N / (ms / 1e3),
             "unit": "fwd+inv functions/s", "ms_per_step": ms, "coeff_err_vs_fp64": err}
+
+
+def odd_bw_bench(api, torch, stream, seed):
+    """32 real functions at bw 255 (odd: length-510 DFTs as Bluestein convolutions) on the plain
+    FP64 path, fwd+inv, with the round-trip error."""
+    B, N = 255, 32
+    rc, ic = real_field_coeffs(np.random.default_rng(seed + 255), B, 1.0, N)
+    plan = api.Plan(B, B)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    g = torch.empty(N, 4 * B * B, dtype=torch.float64, device="cuda")
+    o_r, o_i = torch.empty_like(d_rc), torch.empty_like(d_ic)
+
+    def step():
+        plan.inv_fst(d_rc, d_ic, g, None, N, api.REAL, stream)
+        plan.fst(g, None, o_r, o_i, N, api.REAL, stream)
+
+    ms = _time(torch, stream, step, 5)
+    err = (torch.hypot(o_r - d_rc, o_i - d_ic).amax(dim=1) / torch.hypot(d_rc, d_ic).amax(dim=1)).max().item()
+    return {"workload": "32 real functions at bw 255, (1+l)^-1, plain FP64, fwd+inv", "value": N / (ms / 1e3),
+            "unit": "fwd+inv functions/s", "ms_per_step": ms, "roundtrip_err": err}
 
 
 def complex_bench(api, torch, stream, seed):
