@@ -304,7 +304,7 @@ static void table_dct(int bw, const double* in, double* out) {
 /* cospml.c:161-242 -- cosine series of P(m,l) (m even) or G(m,l) = P(m,l)/sin (m odd),
  * l = m..bw-1, sampled at bw Chebyshev nodes, zero-striped entries dropped. */
 void orc_generate_cos_pml_table(int bw, int m, double* table) {
-    double* buf = (double*)malloc(sizeof(double) * 6 * bw);
+    double* buf = (double*)calloc((size_t)6 * bw, sizeof(double));
     double *pp = buf, *p = buf + bw, *cur = buf + 2 * bw, *x = buf + 3 * bw, *th = buf + 4 * bw,
            *cs = buf + 5 * bw;
     for (int i = 0; i < bw; ++i) {

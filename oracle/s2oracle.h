@@ -12,7 +12,7 @@
  *   - the analytic known-answer inputs data/y20_bw8.dat, y31_bw8.dat (and the odd-bandwidth
  *     y43_bw23.dat / yMix_bw17.dat forward cases),
  *   - outputs of the reference C sources compiled here against oracle/fftw_shim
- *     (tests/golden/*.npz, generated by tests/golden/make_golden.py).
+ *     (the tests/golden/ref_*.npz fixtures, generated by tests/golden/make_golden.py).
  *
  * Every function cites the reference file:line it restates (paths relative to the
  * S2kit repository root).  All arithmetic is FP64, as in the reference.

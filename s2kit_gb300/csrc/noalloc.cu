@@ -61,7 +61,7 @@ extern "C" int s2g_fst_noalloc(const double* rdata, const double* idata, double*
         return fail(S2G_ERR_ARG, "s2g_fst_noalloc: NULL argument");
     int dev;
     S2G_CUDA(cudaGetDevice(&dev));
-    double* scratch;
+    double* scratch = nullptr;
     S2G_TRY(noalloc_scratch(dev, &scratch));
     cudaStream_t st = (cudaStream_t)stream;
     const int S = 2 * bw;

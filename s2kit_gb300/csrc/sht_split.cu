@@ -2230,8 +2230,8 @@ static int get_itab(Split* s, bool fwd, int NB, const int2** out, int* per_tile)
 
 int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* counter, int ctas_per_sm,
               cudaStream_t st) {
-    int nprod;
-    bool f16;
+    int nprod = 0;
+    bool f16 = false;
     S2G_TRY(check_prec(precision, &nprod, &f16));
     if (ncls < 1 || ncls > kMaxClasses) return fail(S2G_ERR_ARG, "%d bandwidth classes (1..%d)", ncls, kMaxClasses);
     Leg p{};
@@ -2399,8 +2399,8 @@ static int* work_counter(void* work, int B, int batch) {
 
 int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int precision, void* work,
               cudaStream_t st) {
-    int nprod;
-    bool f16;
+    int nprod = 0;
+    bool f16 = false;
     S2G_TRY(check_prec(precision, &nprod, &f16));
     S2G_TRY(build_split(t));
     Split* s = (Split*)t->split;
@@ -2424,8 +2424,8 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
 
 int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int batch, int precision, void* work,
                   cudaStream_t st) {
-    int nprod;
-    bool f16;
+    int nprod = 0;
+    bool f16 = false;
     S2G_TRY(check_prec(precision, &nprod, &f16));
     const int B = t->bw, S = 2 * B;
     float* F = (float*)work;
@@ -2585,8 +2585,8 @@ int fst_split_complex(Tables* t, const float* rgrid, const float* igrid, float* 
 
 int inv_fst_split_complex(Tables* t, const float* rc, const float* ic, float* rgrid, float* igrid, int batch,
                           int precision, void* work, void* cwork, cudaStream_t st) {
-    int nprod;
-    bool f16;
+    int nprod = 0;
+    bool f16 = false;
     S2G_TRY(check_prec(precision, &nprod, &f16));
     const int B = t->bw;
     const size_t n = (size_t)batch * B * B;
@@ -2619,8 +2619,8 @@ int split_inv_tail(Tables* t, float* F, float* Fc, float* grid, int batch, const
 }
 
 int split_prepare(Tables* t, int precision) {
-    int nprod;
-    bool f16;
+    int nprod = 0;
+    bool f16 = false;
     S2G_TRY(check_prec(precision, &nprod, &f16));
     return f16 ? build_split16(t) : build_split(t);
 }
