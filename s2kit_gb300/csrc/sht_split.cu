@@ -425,6 +425,9 @@ struct FftShape {
     static constexpr int W = 8;
     static constexpr int LAT = 2 * W;
     static constexpr int T = 32 * W;
+    // resident CTAs per SM the rows-inverse kernel is compiled for: register budgets of 128
+    // (R = 32), 64 (R = 16), 48 (R = 8) and 32 (R <= 4) per thread
+    static constexpr int kMinCtasInv = R == 64 ? 1 : R == 32 ? 2 : R == 16 ? 4 : R == 8 ? 5 : 8;
 };
 
 // Shared-memory layouts of the FFT kernels put the 16-byte staged buffers first (per-warp
@@ -738,7 +741,7 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
 // DFT with sign +1 over the orders for LAT latitudes (two real output rows per warp).  The
 // order-major input arrives as float4 runs of 4 latitudes; output rows leave as float4.
 template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
+__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasInv) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
                                                     const float2* __restrict__ gtw,
                                                     const int64_t* __restrict__ gmap) {
     using L = FftSmem<R>;
@@ -813,6 +816,10 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
     };
     float* zr = spr + warp * PSA;
     float* zi = spi + warp * PSA;
+    // the four-step form (R = 8, 16, 32) leaves 32 consecutive outputs in register k1 of the 32
+    // lanes: each store is one full 128-byte line of row a (real parts) or row b (imaginary
+    // parts), straight from registers.  The other forms stage the spectrum for float4 stores.
+    constexpr bool kDirect = R >= 8 && R <= 32;
     if constexpr (R == 64) {
         // both halves' inputs are gathered before the tile dies (its space becomes the spectra)
         float2 ve[32], vo[32];
@@ -827,25 +834,37 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_inv_w(const float* __re
         float2 v[R];
 #pragma unroll
         for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
-        __syncthreads();  // the tile is dead: spectrum buffers below overwrite it
+        __syncthreads();  // the tile is dead: the exchange planes and spectra below overwrite it
         WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
+        if constexpr (kDirect) {
+            float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;
 #pragma unroll
-        for (int k1 = 0; k1 < R; ++k1) {
-            const int o = pad32(WarpFFTSel<R>::out_index(k1));
-            zr[o] = v[k1].x;
-            zi[o] = v[k1].y;
+            for (int k1 = 0; k1 < R; ++k1) {
+                const int o = WarpFFTSel<R>::out_index(k1);
+                ga[o] = v[k1].x;
+                ga[S + o] = v[k1].y;
+            }
+        } else {
+#pragma unroll
+            for (int k1 = 0; k1 < R; ++k1) {
+                const int o = pad32(WarpFFTSel<R>::out_index(k1));
+                zr[o] = v[k1].x;
+                zi[o] = v[k1].y;
+            }
         }
     }
-    __syncwarp();
-    float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;
-    for (int e = lane; e < S / 4; e += 32) {
-        const int k = 4 * e;
-        reinterpret_cast<float4*>(ga)[e] =
-            make_float4(zr[pad32(k)], zr[pad32(k + 1)], zr[pad32(k + 2)], zr[pad32(k + 3)]);
-        reinterpret_cast<float4*>(ga + S)[e] =
-            make_float4(zi[pad32(k)], zi[pad32(k + 1)], zi[pad32(k + 2)], zi[pad32(k + 3)]);
+    if constexpr (!kDirect) {
+        __syncwarp();
+        float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;
+        for (int e = lane; e < S / 4; e += 32) {
+            const int k = 4 * e;
+            reinterpret_cast<float4*>(ga)[e] =
+                make_float4(zr[pad32(k)], zr[pad32(k + 1)], zr[pad32(k + 2)], zr[pad32(k + 3)]);
+            reinterpret_cast<float4*>(ga + S)[e] =
+                make_float4(zi[pad32(k)], zi[pad32(k + 1)], zi[pad32(k + 2)], zi[pad32(k + 3)]);
+        }
     }
-    __syncthreads();  // the spectra (aliasing the tile) are read before the next tile is loaded
+    __syncthreads();  // the exchange planes and spectra (aliasing the tile) are done before the next tile is loaded
     }
 }
 
