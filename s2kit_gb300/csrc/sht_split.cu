@@ -444,6 +444,10 @@ struct FftSmem {
     // B = 16) spreads a warp's float4-component stores (8 orders x 4 latitude groups) over 32 banks,
     // and the per-warp gathers of one latitude over consecutive orders are conflict-free
     static constexpr int TS = B + 2;
+    // the inverse DCT kernel's per-warp prefetch rows: two planes of PB floats.  R <= 16 only: at
+    // R = 32 the 34 KB they add leave one CTA per SM (+4% there against -7% at R = 16)
+    static constexpr bool kDctInvPf = R <= 16;
+    static constexpr int PB = B + 16;
     // the four-step warp FFT exchanges through the warp's spectrum rows
     static_assert((R != 8 && R != 16 && R != 32) || R * (32 + 32 / R) <= PSA, "exchange planes fit the spectrum rows");
     // R = 64 (WarpFFT2048): the odd pass exchanges in [OFF, OFF + 32 * 33), the spectrum reaches pad32(2047)
@@ -640,9 +644,15 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     constexpr int S = L::S, B = L::B, PSA = L::PSA;
     constexpr int W = FftShape<R>::W;
     extern __shared__ __align__(16) float fsm[];
+    // R <= 16: each warp's next row of Fc is copied into its prefetch buffer while the current
+    // row is transformed (the global loads' latency was this kernel's main stall).  Per plane: the t = 0 half at 0, the t = 1 half at B/2 + 16 (PB floats
+    // per plane), so that the even and odd lanes' reads fall in different banks.
+    constexpr bool kPf = L::kDctInvPf;
+    constexpr int PB = L::PB;
     float* spr = fsm;                  // [W][PSA]
     float* spi = spr + W * PSA;        // [W][PSA]
-    float* sn = spi + W * PSA;         // S
+    float* pfb = spi + W * PSA;        // [W][2][PB] (kPf)
+    float* sn = pfb + (kPf ? W * 2 * PB : 0);  // S
     float2* twD = reinterpret_cast<float2*>(sn + S);
     float2* tw = twD + S;
     float2* twb = tw + (R == 64 ? twtab_len(S / 2) : twtab_len(S));
@@ -658,10 +668,26 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* zr = spr + warp * PSA;
     float* zi = spi + warp * PSA;
+    float* pf = pfb + warp * 2 * PB;
+    const int rstride = gridDim.x * W;
+    // asynchronous copy of row r's two planes (B/4 16-byte pieces each) into the warp's buffer;
+    // naive-order rows and rows past the end copy nothing.  One commit group per call.
+    auto prefetch = [&](int r) {
+        if (r < nrows && !naive_order(r % B)) {
+            for (int c = lane; c < B / 2; c += 32) {
+                const int pl = c >= B / 4, q = 4 * (c - pl * (B / 4));
+                tc::cp_async16(pf + pl * PB + q + (q >= B / 2 ? 16 : 0), Fc + (size_t)(pl * nrows + r) * B + q, 16u);
+            }
+        }
+        tc::cp_async_commit();
+    };
+    if constexpr (kPf) prefetch(blockIdx.x * W + warp);
     // persistent: the tables are loaded once, then each warp walks rows
-    for (int row = blockIdx.x * W + warp; row < nrows; row += gridDim.x * W) {
+    for (int row = blockIdx.x * W + warp; row < nrows; row += rstride) {
     const int m = row % B;
     if (naive_order(m)) {
+        // the buffer is idle during a naive row: the next row's copy starts now
+        if constexpr (kPf) prefetch(row + rstride);
         // Naive orders: the contraction left D0 (even l - m) in F[..][0, B) and D1 (odd l - m) in
         // F[..][B, 2B) for the northern latitudes; P(m,l)(-x) = (-1)^(l-m) P(m,l)(x) gives
         // F[theta] = D0 + D1 and F[2B-1-theta] = D0 - D1 (times 1/sqrt(2 pi)), in place.
@@ -689,12 +715,14 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
         __syncwarp();
         continue;
     }
-    // Fc[p][f][m][t][j]: cosine coefficient k = 2j + t at (k & 1) * B/2 + k/2
-    const float* xa = Fc + (size_t)row * B;
-    const float* xb = Fc + (size_t)(nrows + row) * B;
+    // Fc[p][f][m][t][j]: cosine coefficient k = 2j + t at (k & 1) * B/2 + k/2 (in the prefetch
+    // buffer: (k & 1) * (B/2 + 16) + k/2)
+    const float* xa = kPf ? pf : Fc + (size_t)row * B;
+    const float* xb = kPf ? pf + PB : Fc + (size_t)(nrows + row) * B;
+    constexpr int HO = kPf ? B / 2 + 16 : B / 2;
     auto in = [&](int k) {
         const int r = S - k;
-        const int ok = (k & 1) * (B / 2) + (k >> 1), orr = (r & 1) * (B / 2) + (r >> 1);
+        const int ok = (k & 1) * HO + (k >> 1), orr = (r & 1) * HO + (r >> 1);
         const float ak = (k < B) ? xa[ok] : 0.f, bk = (k < B) ? xb[ok] : 0.f;
         const float ar = (k > 0 && r < B) ? xa[orr] : 0.f, br = (k > 0 && r < B) ? xb[orr] : 0.f;
         const float wr = ak + br, wi = bk - ar;
@@ -705,8 +733,16 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
         WarpFFT2048::to_spectrum(in, tw, twb, twc, zr, zi, 1.f);
     } else {
         float2 v[R];
+        if constexpr (kPf) {
+            tc::cp_async_wait(0);  // this lane's copies of the row have landed
+            __syncwarp();          // and every lane's
+        }
 #pragma unroll
         for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
+        if constexpr (kPf) {
+            __syncwarp();  // the buffer is read: the next row's copy may overwrite it
+            prefetch(row + rstride);
+        }
         WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
 #pragma unroll
         for (int k1 = 0; k1 < R; ++k1) {
@@ -2378,7 +2414,8 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
         k_dct_fwd_w<R><<<g, kThreads, smem, st>>>((float*)in, (float*)out, nrows, s->w32,
                                                                         s->twS, s->twD);
     } else if (which == 2) {  // DCT-III
-        smem = spec + sizeof(float) * S + sizeof(float2) * S + tw_bytes;
+        smem = spec + (L::kDctInvPf ? sizeof(float) * kWarps * 2 * L::PB : 0) + sizeof(float) * S +
+               sizeof(float2) * S + tw_bytes;
         S2G_TRY(set_smem((const void*)k_dct_inv_w<R>, smem));
         int g;
         S2G_TRY(persistent_grid((const void*)k_dct_inv_w<R>, kThreads, smem, (nrows + kWarps - 1) / kWarps, &g));
