@@ -594,8 +594,25 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
         WarpFFT2048::to_spectrum(in, tw, twb, twc, wr, wi, -1.f);
     } else {
         float2 v[R];
+        if constexpr (R == 8 || R == 32) {
+            // input j = L + 32 i < S/2 is sample 2j; sample 2j + 1 is the input S-1-j = (31-L) +
+            // 32 (R-1-i) of lane 31 - L.  One 8-byte load per plane feeds both, the odd half
+            // crossing lanes by one shuffle.  Measured faster at R = 8 and 32 (-7%, -9%); at
+            // R = 16 the 4-byte loads below are (-7%: that kernel then keeps 80 registers, 3 CTAs)
 #pragma unroll
-        for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
+            for (int i = 0; i < R / 2; ++i) {
+                const int q = 2 * (lane + 32 * i);
+                const float2 a = *reinterpret_cast<const float2*>(xr + q);
+                const float2 b = *reinterpret_cast<const float2*>(xi + q);
+                const float2 w2 = *reinterpret_cast<const float2*>(ws + q);
+                v[i] = make_float2(a.x * w2.x, b.x * w2.x);
+                v[R - 1 - i].x = __shfl_xor_sync(0xffffffffu, a.y * w2.y, 31);
+                v[R - 1 - i].y = __shfl_xor_sync(0xffffffffu, b.y * w2.y, 31);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
+        }
         WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
 #pragma unroll
         for (int k1 = 0; k1 < R; ++k1) {
