@@ -485,6 +485,11 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
     const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + 2 * warp) * S;
     float* wr = spr + warp * PSA;
     float* wi = spi + warp * PSA;
+    // R = 8, 16, 32: the spectrum as (re, im) pairs, Z[k] (k < B) at wr[2 pad32(k)] and Z[k]
+    // (k >= B) at wi[2 pad32(k - B)] (the warp's two plane segments), so that the output phase
+    // reads each value with one 8-byte load (-1 to -2%).  Otherwise planes wr/wi[pad32(k)] (at
+    // R <= 4 the pairs cost registers and occupancy: +14% at R = 4).
+    constexpr bool kPairSpec = R >= 8 && R <= 32;
     if constexpr (R == 64) {
         WarpFFT2048::to_spectrum([&](int j) { return make_float2(ra[j], ra[S + j]); }, tw, twb, twc, wr, wi, -1.f);
     } else {
@@ -494,9 +499,13 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
         WarpFFTSel<R>::run(v, tw, twb, wr, wi, -1.f);
 #pragma unroll
         for (int k1 = 0; k1 < R; ++k1) {
-            const int o = pad32(WarpFFTSel<R>::out_index(k1));
-            wr[o] = v[k1].x;
-            wi[o] = v[k1].y;
+            const int o = WarpFFTSel<R>::out_index(k1);
+            if constexpr (kPairSpec) {
+                *reinterpret_cast<float2*>((o < B ? wr + 2 * pad32(o) : wi + 2 * pad32(o - B))) = v[k1];
+            } else {
+                wr[pad32(o)] = v[k1].x;
+                wi[pad32(o)] = v[k1].y;
+            }
         }
     }
     __syncthreads();
@@ -505,13 +514,22 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
     const float hs = 0.5f * scale;
     for (int e = threadIdx.x; e < B * Q4; e += T) {
         const int m = e / Q4, q = 4 * (e - m * Q4);
-        const int pm = pad32(m), pmm = pad32((S - m) & (S - 1));
+        const int pm = pad32(m);
         float re[4], im[4];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {  // latitude pair q/2 + h is warp q/2 + h's (a, b) rows
             const float* zr = spr + (q / 2 + h) * PSA;
             const float* zi = spi + (q / 2 + h) * PSA;
-            const float ar = zr[pm], ai = zi[pm], br = zr[pmm], bi = zi[pmm];
+            float ar, ai, br, bi;
+            if constexpr (!kPairSpec) {
+                const int pmm = pad32((S - m) & (S - 1));
+                ar = zr[pm], ai = zi[pm], br = zr[pmm], bi = zi[pmm];
+            } else {
+                // Z[m] (m < B) and Z[S - m] (S - m > B, or Z[0] for m = 0)
+                const float2 zm = *reinterpret_cast<const float2*>(zr + 2 * pm);
+                const float2 zn = m == 0 ? zm : *reinterpret_cast<const float2*>(zi + 2 * pad32(B - m));
+                ar = zm.x, ai = zm.y, br = zn.x, bi = zn.y;
+            }
             re[2 * h] = (ar + br) * hs;
             im[2 * h] = (ai - bi) * hs;
             re[2 * h + 1] = (ai + bi) * hs;
@@ -802,11 +820,17 @@ __global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasInv) k_ro
     constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
     static_assert(S % LAT == 0 && LAT % 4 == 0, "row staging");
     extern __shared__ __align__(16) float fsm[];
-    // the latitude-major tile [LAT][TS] (re, im) is dead once every warp holds its inputs; the warps'
-    // spectrum buffers [W][PSA] (re, im) then reuse the same space
+    // R = 8, 16: the tile (re, im) holds latitude pairs: latitude th0 + lat of order m at
+    // [(lat / 2) * PS + 2 m + (lat & 1)], PS = 2 TS = 2B + 4 floats (4 mod 32), so that a float4 of 4
+    // latitudes goes in as two conflict-free 8-byte stores and a warp reads its pair (a, b) of one
+    // order with one 8-byte load per plane (-2% at R = 16; +2-3% at R = 4 and 32, which keep the
+    // latitude-major [LAT][TS]).  Either tile is dead once every warp holds its inputs; the warps'
+    // spectrum buffers [W][PSA] (re, im) then reuse the same space.
+    constexpr bool kPairTile = R == 8 || R == 16;
+    constexpr int PS = 2 * TS;
     constexpr int U = 2 * LAT * TS > 2 * W * PSA ? 2 * LAT * TS : 2 * W * PSA;
     float* tr = fsm;
-    float* ti = tr + LAT * TS;
+    float* ti = tr + (LAT / 2) * PS;
     float* spr = fsm;
     float* spi = spr + W * PSA;
     float2* tw = reinterpret_cast<float2*>(fsm + U);
@@ -842,28 +866,46 @@ __global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasInv) k_ro
             const int e = threadIdx.x + (it0 + u) * T;
             if (e < B * Q4) {
                 const int m = e / Q4, q = 4 * (e - m * Q4);
-                float* pr = tr + q * TS + m;
-                float* pi = ti + q * TS + m;
-                pr[0] = a[u].x, pr[TS] = a[u].y, pr[2 * TS] = a[u].z, pr[3 * TS] = a[u].w;
-                pi[0] = b[u].x, pi[TS] = b[u].y, pi[2 * TS] = b[u].z, pi[3 * TS] = b[u].w;
+                if constexpr (kPairTile) {
+                    float* pr = tr + (q / 2) * PS + 2 * m;
+                    float* pi = ti + (q / 2) * PS + 2 * m;
+                    *reinterpret_cast<float2*>(pr) = make_float2(a[u].x, a[u].y);
+                    *reinterpret_cast<float2*>(pr + PS) = make_float2(a[u].z, a[u].w);
+                    *reinterpret_cast<float2*>(pi) = make_float2(b[u].x, b[u].y);
+                    *reinterpret_cast<float2*>(pi + PS) = make_float2(b[u].z, b[u].w);
+                } else {
+                    float* pr = tr + q * TS + m;
+                    float* pi = ti + q * TS + m;
+                    pr[0] = a[u].x, pr[TS] = a[u].y, pr[2 * TS] = a[u].z, pr[3 * TS] = a[u].w;
+                    pi[0] = b[u].x, pi[TS] = b[u].y, pi[2 * TS] = b[u].z, pi[3 * TS] = b[u].w;
+                }
             }
         }
     }
     __syncthreads();
-    const int a = 2 * warp, b = a + 1;
+    const int a = 2 * warp, b = a + 1;  // this warp's latitudes (pair row `warp` of a pair tile)
+    // latitudes a and b of order mm < B: (re_a, re_b) and (im_a, im_b)
+    auto at = [&](int mm, float2& re, float2& im) {
+        if constexpr (kPairTile) {
+            re = *reinterpret_cast<const float2*>(tr + warp * PS + 2 * mm);
+            im = *reinterpret_cast<const float2*>(ti + warp * PS + 2 * mm);
+        } else {
+            re = make_float2(tr[a * TS + mm], tr[b * TS + mm]);
+            im = make_float2(ti[a * TS + mm], ti[b * TS + mm]);
+        }
+    };
     auto in = [&](int m) {
         float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
+        float2 re, im;
         if (m < B) {
-            ar = tr[a * TS + m];
-            ai = (m == 0) ? 0.f : ti[a * TS + m];
-            br = tr[b * TS + m];
-            bi = (m == 0) ? 0.f : ti[b * TS + m];
+            at(m, re, im);
+            ar = re.x, br = re.y;
+            ai = (m == 0) ? 0.f : im.x;
+            bi = (m == 0) ? 0.f : im.y;
         } else if (m > B) {
-            const int mm = S - m;
-            ar = tr[a * TS + mm];
-            ai = -ti[a * TS + mm];
-            br = tr[b * TS + mm];
-            bi = -ti[b * TS + mm];
+            at(S - m, re, im);
+            ar = re.x, br = re.y;
+            ai = -im.x, bi = -im.y;
         }
         return make_float2(ar - bi, ai + br);  // F_a + i F_b
     };
