@@ -547,7 +547,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __re
 // C[p][f][m][t][j] holds frequency k = 2j + t (j < B/2), so that the contraction's operand rows
 // of one parity are contiguous.  Naive orders are folded in place in X for their contraction:
 // X[p][f][m][t][j] = x[j] + (-1)^t x[S-1-j], j < B (the even/odd latitude halves).
-// Rows are read and written in 16-byte pieces through the warp's spectrum buffers.
+// Seminaive rows are read straight into the FFT's registers (4- or 8-byte loads) and leave in
+// 16-byte pieces through the warp's spectrum buffer; naive rows go through it both ways.
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict__ X, float* __restrict__ Cout, int nrows,
                                                    const float* __restrict__ gw, const float2* __restrict__ gtw,
@@ -670,7 +671,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
 }
 
 // REDFT01 per (function, seminaive order) row, sin(theta) for odd m, scale: F[p][f][m][theta].
-// Rows are read and written in 16-byte pieces through the warp's spectrum buffers.
+// Seminaive rows arrive through the warp's cp.async prefetch buffer (R <= 16) or straight from
+// global memory, and leave in 16-byte pieces through the warp's spectrum buffer.
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
                                                    const float* __restrict__ gsin, const float2* __restrict__ gtw,
@@ -810,7 +812,8 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
 }
 
 // DFT with sign +1 over the orders for LAT latitudes (two real output rows per warp).  The
-// order-major input arrives as float4 runs of 4 latitudes; output rows leave as float4.
+// order-major input arrives as float4 runs of 4 latitudes; output rows leave as 128-byte lines
+// from registers (R = 8, 16, 32) or as float4 through the warp's spectrum buffer.
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasInv) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
                                                     const float2* __restrict__ gtw,
