@@ -177,8 +177,9 @@ struct WarpFFT {
 
 // Four-step form of the same transform for R in {8, 16, 32}: stages (a) and (b) as above, then the
 // 32-point DFTs across the lanes go through shared memory instead of lane butterflies.
-//   (c1) lane l writes u_l[k1] to row k1, column l of the warp's exchange planes (row stride
-//        32 + P floats, P = 32 / R: conflict-free in both directions);
+//   (c1) lane l writes u_l[k1] to row k1, column l of the warp's exchange rows: (re, im) pairs,
+//        row stride 32 + P pairs (P = 32 / R), rows k1 < R/2 in the first plane and the others
+//        in the second (conflict-free 8-byte accesses in both directions);
 //   (c2) lane L = P c + h reads column c at lanes P j + h (j < R): y_j = u_{P j + h}[c], and
 //        takes their R-point DFT in registers, Y_h[k] = sum_j y_j w_R^(j k);
 //   (c3) Z_c[k + R q] = sum_h T_h[k] w_P^(h q) with T_h[k] = w_32^(h k) Y_h[k]: a P-point DFT
@@ -190,7 +191,7 @@ struct WarpFFT {
 //        for every q.
 // Then X[c + R k2] = Z_c[k2].  Register s of lane L holds X[out_index(s)], and for a fixed s the
 // 32 lanes hold 32 consecutive indices, so spectrum stores through pad32 are conflict-free.
-// Shared-memory traffic per transform: R exchange writes and reads per plane and log2(P) R
+// Shared-memory traffic per transform: R 8-byte exchange writes and R reads, and log2(P) R
 // shuffles, against 10 R shuffles of the lane-butterfly form.
 // u[K] *= w_32^(h K), K = K0 .. R-1, for a runtime h in 1 .. P-1 (P <= 4): the P-1 candidate
 // factors of each K are compile-time constants and h selects one.
@@ -271,19 +272,20 @@ struct WarpFFT4 {
             w.y *= sign;
             u[k1] = cmulf(u[k1], w);
         }
-        // (c1) exchange
+        // (c1) exchange: (re, im) pairs, row k1 < R/2 in xr and row k1 >= R/2 in xi, each row XS
+        // pairs long (R XS floats per plane, as two planes of single floats would take); one
+        // 8-byte store per value, conflict-free
         __syncwarp();
 #pragma unroll
-        for (int k1 = 0; k1 < R; ++k1) {
-            xr[k1 * XS + lane] = u[k1].x;
-            xi[k1 * XS + lane] = u[k1].y;
-        }
+        for (int k1 = 0; k1 < R; ++k1)
+            *reinterpret_cast<float2*>((k1 < R / 2 ? xr : xi) + 2 * ((k1 % (R / 2)) * XS + lane)) = u[k1];
         __syncwarp();
-        // (c2) column c, lanes P j + h, R-point DFT in registers
+        // (c2) column c, lanes P j + h, R-point DFT in registers; one 8-byte load per value, the
+        // half-warp's 16 lanes on 16 distinct 8-byte bank pairs (XS = 32 + P)
         const int c = lane / P, h = lane % P;
+        const float* xrow = (c < R / 2 ? xr + 2 * c * XS : xi + 2 * (c - R / 2) * XS) + 2 * h;
 #pragma unroll
-        for (int j = 0; j < R; ++j)
-            u[WarpFFT<R>::brev(j)] = make_float2(xr[c * XS + P * j + h], xi[c * XS + P * j + h]);
+        for (int j = 0; j < R; ++j) u[WarpFFT<R>::brev(j)] = *reinterpret_cast<const float2*>(xrow + 2 * P * j);
         __syncwarp();  // the exchange planes are free again (callers reuse them)
         RegStages<R, 2>::run(u, sign);
         if constexpr (P > 1) {

@@ -428,6 +428,9 @@ struct FftShape {
     // resident CTAs per SM the rows-inverse kernel is compiled for: register budgets of 128
     // (R = 32), 64 (R = 16), 48 (R = 8) and 32 (R <= 4) per thread
     static constexpr int kMinCtasInv = R == 64 ? 1 : R == 32 ? 2 : R == 16 ? 4 : R == 8 ? 5 : 8;
+    // the rows-forward kernel: 48 registers at R = 8 (5 CTAs per SM; unbounded it takes 62 and
+    // runs 4% slower); 0 leaves the other lengths unbounded
+    static constexpr int kMinCtasFwd = R == 8 ? 5 : 0;
 };
 
 // Shared-memory layouts of the FFT kernels put the 16-byte staged buffers first (per-warp
@@ -459,7 +462,7 @@ struct FftSmem {
 // X_a = (Z[m] + conj Z[S-m]) / 2 and X_b = (Z[m] - conj Z[S-m]) / 2i, is done by the threads
 // that write the transposed tile, each a float4 run of 4 latitudes of one order.
 template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T) k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N,
+__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasFwd) k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N,
                                                     float scale, const float2* __restrict__ gtw,
                                                     const int64_t* __restrict__ gmap) {
     using L = FftSmem<R>;
