@@ -317,6 +317,9 @@ def main():
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    for k, v in kern.items():  # every kernel's algorithmic bytes over its event-timed duration
+        kb = algorithmic_bytes(k, B, N)
+        v["hbm_frac"] = kb / (v["avg_ms"] / 1e3) / 1e9 / hbm_peak if kb else None
     ab = algorithmic_bytes(dom, B, N)
     achieved = ab / (kern[dom]["avg_ms"] / 1e3) / 1e9 if ab else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
