@@ -685,8 +685,9 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     constexpr int W = FftShape<R>::W;
     extern __shared__ __align__(16) float fsm[];
     // R <= 16: each warp's next row of Fc is copied into its prefetch buffer while the current
-    // row is transformed (the global loads' latency was this kernel's main stall).  Per plane: the t = 0 half at 0, the t = 1 half at B/2 + 16 (PB floats
-    // per plane), so that the even and odd lanes' reads fall in different banks.
+    // row is transformed (the global loads' latency was this kernel's main stall).  Per plane:
+    // the t = 0 half at 0, the t = 1 half at B/2 + 16 (PB floats per plane), so that the even and
+    // odd lanes' reads fall in different banks.
     constexpr bool kPf = L::kDctInvPf;
     constexpr int PB = L::PB;
     float* spr = fsm;                  // [W][PSA]
