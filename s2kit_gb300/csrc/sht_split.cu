@@ -462,9 +462,9 @@ struct FftSmem {
 // X_a = (Z[m] + conj Z[S-m]) / 2 and X_b = (Z[m] - conj Z[S-m]) / 2i, is done by the threads
 // that write the transposed tile, each a float4 run of 4 latitudes of one order.
 template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasFwd) k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N,
-                                                    float scale, const float2* __restrict__ gtw,
-                                                    const int64_t* __restrict__ gmap) {
+__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasFwd)
+    k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N, float scale,
+                 const float2* __restrict__ gtw, const int64_t* __restrict__ gmap) {
     using L = FftSmem<R>;
     constexpr int S = L::S, B = L::B, PSA = L::PSA;
     constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
@@ -819,9 +819,9 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
 // order-major input arrives as float4 runs of 4 latitudes; output rows leave as 128-byte lines
 // from registers (R = 8, 16, 32) or as float4 through the warp's spectrum buffer.
 template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasInv) k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N,
-                                                    const float2* __restrict__ gtw,
-                                                    const int64_t* __restrict__ gmap) {
+__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasInv)
+    k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N, const float2* __restrict__ gtw,
+                 const int64_t* __restrict__ gmap) {
     using L = FftSmem<R>;
     constexpr int S = L::S, B = L::B, PSA = L::PSA, TS = L::TS;
     constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
