@@ -243,7 +243,9 @@ int s2g_inv_fst_refined(s2g_plan plan, const double* rcoeffs, const double* icoe
  * twiddle factors live in a fixed __device__ array of about 4 MiB held by every GPU that loads
  * the library.  All pointers are device pointers: samples, coefficients (as s2g_fst), the
  * seminaive/naive table in the SemiNaive_Naive_Pml_Table layout with its bw int64 order offsets,
- * and the 4*bw quadrature weights.  bw <= 256; larger bw is rejected with S2G_ERR_ARG.  The first
+ * and the 4*bw quadrature weights.  bw <= 256 (any such bw: when 2*bw is not a power of two
+ * the Bluestein tables of its DFTs are rewritten into the array on every call); larger bw is
+ * rejected with S2G_ERR_ARG.  The first
  * call on a device looks up the array's device address (make that first call before any stream
  * capture).  Calls share the array, so calls that overlap on the GPU race: serialise them. */
 int s2g_fst_noalloc(const double* rdata, const double* idata, double* rcoeffs, double* icoeffs, int bw,

@@ -108,6 +108,12 @@ struct F64Work {
 size_t f64_work_bytes(int bw, int batch, int data_format);
 int fst_f64(const Tables* t, const double* rdata, const double* idata, double* rc, double* ic, int batch,
             int data_format, int cutoff, void* work, cudaStream_t st);
+// fst_f64 with the DFT geometry of length 2bw (Bluestein tables included when 2bw is not a
+// power of two) supplied by the caller instead of looked up in the per-device length cache,
+// which builds missing tables with cudaMalloc.  Null `len_S` behaves like fst_f64.
+struct Len;
+int fst_f64_len(const Tables* t, const Len* len_S, const double* rdata, const double* idata, double* rc,
+                double* ic, int batch, int data_format, int cutoff, void* work, cudaStream_t st);
 int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rdata, double* idata, int batch,
                 int data_format, int cutoff, void* work, cudaStream_t st);
 int fzt_f64(const Tables* t, const double* rdata, const double* idata, double* rres, double* ires, int batch,

@@ -494,11 +494,16 @@ static size_t rows_smem(const Len& L, int R) {
     return ((size_t)2 * R * (L.n + 1) + L.tmp_len()) * sizeof(double);
 }
 
+// `given`: the geometry of length 2B (with its Bluestein tables) built by the caller; null looks
+// it up (and builds it on first use) with dft_len.
 static int launch_rows_fwd(const double* rdata, const double* idata, double* Xr, double* Xi, int B, int rows_out,
-                           int batch, const double2* tw, cudaStream_t st) {
+                           int batch, const double2* tw, cudaStream_t st, const Len* given = nullptr) {
     const int S = 2 * B;
     Len L;
-    S2G_TRY(dft_len(S, &L));
+    if (given)
+        L = *given;
+    else
+        S2G_TRY(dft_len(S, &L));
     const int R = rows_per_cta(S);
     const int lat_per = idata ? R : 2 * R;
     const size_t smem = rows_smem(L, R);
@@ -523,9 +528,12 @@ static int pick_group(int B, int S, bool naive, int tmp_len, size_t* smem_out, s
     return G;
 }
 
-static int launch_fwd_dlt(FwdDlt p, int nrows_grid, cudaStream_t st) {
+static int launch_fwd_dlt(FwdDlt p, int nrows_grid, cudaStream_t st, const Len* given = nullptr) {
     Len L;
-    S2G_TRY(dft_len(p.S, &L));
+    if (given)
+        L = *given;
+    else
+        S2G_TRY(dft_len(p.S, &L));
     size_t smem = 0;
     const bool any_naive = p.one_d ? (p.m1d >= p.cutoff) : (p.cutoff < p.B);
     const int G = pick_group(p.B, p.S, any_naive, L.tmp_len(), &smem);
@@ -573,12 +581,17 @@ size_t f64_work_bytes(int bw, int batch, int data_format) {
 
 int fst_f64(const Tables* t, const double* rdata, const double* idata, double* rc, double* ic, int batch,
             int data_format, int cutoff, void* work, cudaStream_t st) {
+    return fst_f64_len(t, nullptr, rdata, idata, rc, ic, batch, data_format, cutoff, work, st);
+}
+
+int fst_f64_len(const Tables* t, const Len* len_S, const double* rdata, const double* idata, double* rc,
+                double* ic, int batch, int data_format, int cutoff, void* work, cudaStream_t st) {
     const int B = t->bw, S = 2 * B;
     const int rows = (data_format == COMPLEX) ? S : B;
     double* Xr = (double*)work;
     double* Xi = Xr + (size_t)batch * rows * S;
     // REAL data with no imaginary samples: the packed real path (imaginary part zero)
-    S2G_TRY(launch_rows_fwd(rdata, idata, Xr, Xi, B, rows, batch, t->tw_S, st));
+    S2G_TRY(launch_rows_fwd(rdata, idata, Xr, Xi, B, rows, batch, t->tw_S, st, len_S));
     FwdDlt p{};
     p.Xr = Xr;
     p.Xi = Xi;
@@ -597,7 +610,7 @@ int fst_f64(const Tables* t, const double* rdata, const double* idata, double* r
     p.nfunc = batch;
     p.complex_rows = (data_format == COMPLEX);
     p.real_mirror = (data_format != COMPLEX);
-    return launch_fwd_dlt(p, (data_format == COMPLEX) ? S - 1 : B, st);
+    return launch_fwd_dlt(p, (data_format == COMPLEX) ? S - 1 : B, st, len_S);
 }
 
 int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rdata, double* idata, int batch,

@@ -40,7 +40,7 @@ def _call(lib, rd, idd, rc, ic, bw, tab, off, w, fmt, cutoff):
     assert st == 0, lib.s2g_last_error()
 
 
-@pytest.mark.parametrize("bw,cutoff", [(64, 64), (256, 256), (32, 8)])
+@pytest.mark.parametrize("bw,cutoff", [(64, 64), (256, 256), (32, 8), (48, 48), (255, 40)])
 def test_noalloc_matches_fst_twice(bw, cutoff):
     import torch
     lib = s2.load()
@@ -60,6 +60,44 @@ def test_noalloc_matches_fst_twice(bw, cutoff):
         torch.cuda.synchronize()
         assert torch.isfinite(rc).all() and torch.isfinite(ic).all(), f"call {call}"
         err = rel_err_norm(rc.cpu().numpy(), ic.cpu().numpy(), ref_r.cpu().numpy(), ref_i.cpu().numpy())
+        assert err <= TOL, (call, err)
+
+
+def _noalloc_inputs(torch, rng, bw):
+    n = 2 * bw
+    rd = torch.from_numpy(rng.standard_normal(n * n)).cuda()
+    idd = torch.from_numpy(rng.standard_normal(n * n)).cuda()
+    rc = torch.full((bw * bw,), float("nan"), dtype=torch.float64, device="cuda")
+    return rd, idd, rc, torch.full_like(rc, float("nan"))
+
+
+def test_noalloc_non_power_of_two_allocates_nothing(oracle):
+    """A bandwidth whose 2 bw is not a power of two: the length-2bw DFTs are Bluestein
+    convolutions, whose tables the other entry points build with cudaMalloc on the first use of
+    each length.  Here free device memory must not change across the first call at a length no
+    other call in this process has used (bw 100, 2 bw = 200), and both calls in a row (REAL, then
+    COMPLEX) must match the oracle to the FP64 parity bar."""
+    import torch
+    lib = s2.load()
+    rng = np.random.default_rng(7)
+    # a first call at another non-power-of-two length loads this library's kernels and looks up
+    # the scratch array's address (module loading may reserve device memory once per process)
+    tab, off, w = _device_tables(torch, 24, 24)
+    rd, idd, rc, ic = _noalloc_inputs(torch, rng, 24)
+    _call(lib, rd, idd, rc, ic, 24, tab, off, w, api.REAL, 24)
+    bw, cutoff = 100, 100
+    tab, off, w = _device_tables(torch, bw, cutoff)
+    inputs = [_noalloc_inputs(torch, rng, bw) for _ in range(2)]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for (rd, idd, rc, ic), fmt in zip(inputs, (api.REAL, api.COMPLEX)):
+        _call(lib, rd, idd, rc, ic, bw, tab, off, w, fmt, cutoff)
+        torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, (free0, free1)
+    for call, ((rd, idd, rc, ic), fmt) in enumerate(zip(inputs, (api.REAL, api.COMPLEX))):
+        er, ei = oracle.fst(rd.cpu().numpy(), idd.cpu().numpy(), bw, fmt, cutoff)
+        err = rel_err_norm(rc.cpu().numpy(), ic.cpu().numpy(), er, ei)
         assert err <= TOL, (call, err)
 
 
