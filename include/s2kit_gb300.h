@@ -66,9 +66,13 @@ void ConvOn2SphereSemiMemo(double* rdata, double* idata, double* rfilter, double
 
 /* Replace the on-the-fly family, src/FST_semi_fly.c (include/s2kit/FST_semi_fly.h:8-16):
  * FSTSemiFly :67-211, InvFSTSemiFly :235-369, FZTSemiFly :390-425, ConvOn2SphereSemiFly :454-519.
- * The reference generates each order's Legendre table inside every call; here the tables for
- * (bw, cutoff) are generated on the GPU on first use and kept, and the transforms are those of
- * the memo family above.  Workspace and plans are ignored; weights are used when given. */
+ * The reference generates each order's Legendre table inside every call and frees it; here no
+ * table exists on the device at all: the associated Legendre recurrence runs inside the
+ * contraction kernels, which apply the reference's naive Legendre transform (its form for the
+ * orders >= cutoff) to every order.  Results equal the memo family's to rounding; cutoff is
+ * validated and otherwise has no effect.  Device memory per call: the samples, coefficients and
+ * a row-DFT workspace (2 x rows x 2bw doubles), no O(bw^3) table.  Workspace and plans are
+ * ignored; weights are used when given. */
 void FSTSemiFly(double* rdata, double* idata, double* rcoeffs, double* icoeffs, const int bw, double* workspace,
                 DataFormat data_format, const int cutoff, fftw_plan* DCT_plan, fftw_plan* FFT_plan,
                 double* weights);
@@ -173,6 +177,10 @@ typedef struct s2g_plan_s* s2g_plan;
  * a time (one plan per thread for concurrent callers; the tables stay shared). */
 int s2g_plan_create(s2g_plan* plan, int bw, int cutoff);
 int s2g_plan_destroy(s2g_plan plan);
+/* A plan for the on-the-fly family (src/FST_semi_fly.c, as the Fly drop-ins above): it holds no
+ * Legendre table, only weights and twiddles.  s2g_fst, s2g_inv_fst, s2g_fzt and s2g_conv on it
+ * run the on-the-fly kernels; the split-precision entry points reject it (S2G_ERR_ARG). */
+int s2g_plan_create_fly(s2g_plan* plan, int bw);
 /* Device bytes of scratch a call with this batch needs (the plan grows its own scratch
  * on demand when the caller passes none). */
 size_t s2g_plan_workspace_size(s2g_plan plan, int batch, int precision);

@@ -39,9 +39,10 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_ref() -> bool:
-    ref = os.environ.get("S2_REFERENCE_DIR", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src")):
+def build_ref(ref: str | None = None) -> bool:
+    """Builds oracle/_ref from the S2kit checkout at `ref` (or $S2_REFERENCE_DIR); False if absent."""
+    ref = ref or os.environ.get("S2_REFERENCE_DIR", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "src")):
         return False
     with _lock:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True,
@@ -82,6 +83,8 @@ class Oracle:
         L.orc_generate_pml_table.argtypes = [C.c_int, C.c_int, _dp]
         L.orc_tables_new.restype = C.c_void_p
         L.orc_tables_new.argtypes = [C.c_int, C.c_int]
+        L.orc_tables_new_mt.restype = C.c_void_p
+        L.orc_tables_new_mt.argtypes = [C.c_int, C.c_int, C.c_int]
         L.orc_tables_free.argtypes = [C.c_void_p]
         L.orc_tables_total.restype = C.c_int64
         L.orc_tables_total.argtypes = [C.c_void_p]
@@ -100,6 +103,7 @@ class Oracle:
         L.orc_fzt.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp, C.c_int]
         L.orc_transmult.argtypes = [_dp] * 6 + [C.c_int]
         L.orc_conv.argtypes = [_dp] * 6 + [C.c_int]
+        L.orc_conv_tables.argtypes = [_dp] * 6 + [C.c_int, C.c_void_p]
         L.orc_bench_roundtrip.restype = C.c_double
         L.orc_bench_roundtrip.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
         self._tables = {}
@@ -139,13 +143,20 @@ class Oracle:
         """(handle, fwd ndarray view, inv ndarray view, offsets ndarray) cached per (bw, cutoff)."""
         key = (bw, cutoff)
         if key not in self._tables:
-            h = self.lib.orc_tables_new(bw, cutoff)
+            # orders generated on all host cores (identical values to one thread)
+            h = self.lib.orc_tables_new_mt(bw, cutoff, os.cpu_count() or 1)
             n = self.lib.orc_tables_total(h)
             fwd = np.ctypeslib.as_array(self.lib.orc_tables_fwd(h), shape=(max(n, 1),))[:n]
             inv = np.ctypeslib.as_array(self.lib.orc_tables_inv(h), shape=(max(n, 1),))[:n]
             off = np.ctypeslib.as_array(self.lib.orc_tables_offsets(h), shape=(bw,)).copy()
             self._tables[key] = (h, fwd, inv, off)
         return self._tables[key]
+
+    def drop_tables(self, bw: int, cutoff: int) -> None:
+        """Frees the cached tables of (bw, cutoff) (2.9 GB of host memory at bw 1024)."""
+        entry = self._tables.pop((bw, cutoff), None)
+        if entry is not None:
+            self.lib.orc_tables_free(C.c_void_p(entry[0]))
 
     # ---- transforms ----------------------------------------------------------------
     def redft10(self, x: np.ndarray, direct: bool = False) -> np.ndarray:
@@ -231,11 +242,16 @@ class Oracle:
         self.lib.orc_transmult(*[_ptr(a) for a in args], _ptr(rr), _ptr(ir), bw)
         return rr, ir
 
-    def conv(self, rdata, idata, rfilter, ifilter, bw):
+    def conv(self, rdata, idata, rfilter, ifilter, bw, cached_tables: bool = False):
+        """ConvOn2SphereSemiMemo.  With cached_tables the (bw, bw) tables of tables() are used
+        instead of tables built inside the call (same values, no second copy at large bw)."""
         args = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (rdata, idata, rfilter, ifilter)]
         rr = np.empty(4 * bw * bw)
         ir = np.empty(4 * bw * bw)
-        self.lib.orc_conv(*[_ptr(a) for a in args], _ptr(rr), _ptr(ir), bw)
+        if cached_tables:
+            self.lib.orc_conv_tables(*[_ptr(a) for a in args], _ptr(rr), _ptr(ir), bw, self.tables(bw, bw)[0])
+        else:
+            self.lib.orc_conv(*[_ptr(a) for a in args], _ptr(rr), _ptr(ir), bw)
         return rr, ir
 
     def bench_roundtrip(self, bw: int, coeffs: np.ndarray, nthreads: int):
@@ -249,9 +265,9 @@ class Oracle:
 class Reference:
     """The unmodified S2kit C sources (built by `make -C oracle ref`), through their own API."""
 
-    def __init__(self):
-        if not os.path.exists(REF_LIB) and not build_ref():
-            raise RuntimeError("reference checkout not available")
+    def __init__(self, ref: str | None = None):
+        if not os.path.exists(REF_LIB) and not build_ref(ref):
+            raise RuntimeError("reference build not available (oracle/_ref; set S2_REFERENCE_DIR to build it)")
         L = self.lib = C.CDLL(REF_LIB)
         L.TableSize.restype = C.c_int
         L.TableSize.argtypes = [C.c_int, C.c_int]

@@ -380,9 +380,36 @@ void orc_generate_pml_table(int bw, int m, double* table) {
     free(buf);
 }
 
+/* One order of the packed tables: cosine table and its transpose (m < cutoff) or sampled
+ * P(m,l) in both buffers (m >= cutoff). */
+static void tables_order(orc_tables* t, int m) {
+    int bw = t->bw;
+    double* f = t->fwd + t->offsets[m];
+    double* v = t->inv + t->offsets[m];
+    if (m < t->cutoff) {
+        orc_generate_cos_pml_table(bw, m, f);
+        orc_transpose_cos_pml_table(bw, m, f, v);
+    } else {
+        orc_generate_pml_table(bw, m, f);
+        memcpy(v, f, sizeof(double) * 2 * (int64_t)bw * (bw - m));
+    }
+}
+
+typedef struct {
+    orc_tables* t;
+    int tid, nthreads;
+} tables_arg;
+
+static void* tables_worker(void* vp) {
+    tables_arg* a = (tables_arg*)vp;
+    for (int m = a->tid; m < a->t->bw; m += a->nthreads) tables_order(a->t, m);
+    return NULL;
+}
+
 /* cospml.c:451-518 -- seminaive orders m < cutoff (cosine tables), naive orders
- * m >= cutoff (sampled P(m,l)), packed back to back; inverse buffer transposed. */
-orc_tables* orc_tables_new(int bw, int cutoff) {
+ * m >= cutoff (sampled P(m,l)), packed back to back; inverse buffer transposed.  Orders are
+ * independent, so `nthreads` threads may generate them (same values as one thread). */
+orc_tables* orc_tables_new_mt(int bw, int cutoff, int nthreads) {
     orc_tables* t = (orc_tables*)calloc(1, sizeof(orc_tables));
     t->bw = bw;
     t->cutoff = cutoff;
@@ -395,19 +422,27 @@ orc_tables* orc_tables_new(int bw, int cutoff) {
     t->total = off;
     t->fwd = (double*)malloc(sizeof(double) * (off ? off : 1));
     t->inv = (double*)malloc(sizeof(double) * (off ? off : 1));
-    for (int m = 0; m < bw; ++m) {
-        double* f = t->fwd + t->offsets[m];
-        double* v = t->inv + t->offsets[m];
-        if (m < cutoff) {
-            orc_generate_cos_pml_table(bw, m, f);
-            orc_transpose_cos_pml_table(bw, m, f, v);
-        } else {
-            orc_generate_pml_table(bw, m, f);
-            memcpy(v, f, sizeof(double) * 2 * (int64_t)bw * (bw - m));
-        }
+    get_plan(bw);
+    get_plan(4 * bw);
+    if (nthreads <= 1) {
+        for (int m = 0; m < bw; ++m) tables_order(t, m);
+        return t;
     }
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    tables_arg* args = (tables_arg*)malloc(sizeof(tables_arg) * nthreads);
+    for (int i = 0; i < nthreads; ++i) {
+        args[i].t = t;
+        args[i].tid = i;
+        args[i].nthreads = nthreads;
+        pthread_create(&th[i], NULL, tables_worker, &args[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    free(th);
+    free(args);
     return t;
 }
+
+orc_tables* orc_tables_new(int bw, int cutoff) { return orc_tables_new_mt(bw, cutoff, 1); }
 
 void orc_tables_free(orc_tables* t) {
     if (!t) return;
@@ -675,8 +710,16 @@ void orc_transmult(const double* rdatacoeffs, const double* idatacoeffs, const d
 /* FST_semi_memo.c:439-518 -- always REAL, seminaive at every order (cutoff = bw). */
 void orc_conv(const double* rdata, const double* idata, const double* rfilter, const double* ifilter,
               double* rres, double* ires, int bw) {
-    int nc = bw * bw;
     orc_tables* t = orc_tables_new(bw, bw);
+    orc_conv_tables(rdata, idata, rfilter, ifilter, rres, ires, bw, t);
+    orc_tables_free(t);
+}
+
+/* The convolution of orc_conv on tables the caller built (the reference regenerates them in
+ * every call, FST_semi_memo.c:498-500; the values are the same). */
+void orc_conv_tables(const double* rdata, const double* idata, const double* rfilter, const double* ifilter,
+                     double* rres, double* ires, int bw, const orc_tables* t) {
+    int nc = bw * bw;
     double* w = (double*)malloc(sizeof(double) * 4 * bw);
     orc_generate_weights(bw, w);
     double* fr = (double*)malloc(sizeof(double) * (4 * (int64_t)nc + 4 * bw));
@@ -691,7 +734,6 @@ void orc_conv(const double* rdata, const double* idata, const double* rfilter, c
     orc_inv_fst(tr, ti, rres, ires, bw, t, ORC_REAL, bw);
     free(fr);
     free(w);
-    orc_tables_free(t);
 }
 
 /* ===================================================================== */

@@ -70,6 +70,8 @@ typedef struct {
 } orc_tables;
 
 orc_tables* orc_tables_new(int bw, int cutoff);
+/* Same tables, the orders generated by `nthreads` threads (orders interleaved across them). */
+orc_tables* orc_tables_new_mt(int bw, int cutoff, int nthreads);
 void orc_tables_free(orc_tables* t);
 /* Accessors for ctypes callers */
 int64_t orc_tables_total(const orc_tables* t);
@@ -97,6 +99,9 @@ void orc_transmult(const double* rdatacoeffs, const double* idatacoeffs, const d
                    const double* ifiltercoeffs, double* rres, double* ires, int bw);
 void orc_conv(const double* rdata, const double* idata, const double* rfilter, const double* ifilter,
               double* rres, double* ires, int bw);
+/* orc_conv on tables built beforehand (orc_tables_new*(bw, bw)) instead of per call. */
+void orc_conv_tables(const double* rdata, const double* idata, const double* rfilter, const double* ifilter,
+                     double* rres, double* ires, int bw, const orc_tables* t);
 
 /* ---- timed CPU baseline: nfunc independent REAL round trips (InvFST then FST, cutoff=bw),
  * one function per thread at a time, private workspaces, shared read-only tables.

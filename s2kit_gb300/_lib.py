@@ -56,6 +56,7 @@ SIGNATURES = {
     "s2g_cache_clear": (C.c_int, []),
     "s2g_plan_create": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int]),
     "s2g_plan_destroy": (C.c_int, [vp]),
+    "s2g_plan_create_fly": (C.c_int, [C.POINTER(vp), C.c_int]),
     "s2g_plan_workspace_size": (C.c_size_t, [vp, C.c_int, C.c_int]),
     "s2g_fst": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
     "s2g_inv_fst": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),

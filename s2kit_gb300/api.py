@@ -188,14 +188,22 @@ def _stream(s):
 
 
 class Plan:
-    """Batched transforms of bandwidth `bw` on the current CUDA device (s2g_plan)."""
+    """Batched transforms of bandwidth `bw` on the current CUDA device (s2g_plan).
 
-    def __init__(self, bw: int, cutoff: int | None = None):
+    fly=True makes an on-the-fly plan (s2g_plan_create_fly): no Legendre table on the device,
+    the FP64 transforms (fst, inv_fst, fzt, conv) generate the Legendre functions inside their
+    kernels (the FSTSemiFly family)."""
+
+    def __init__(self, bw: int, cutoff: int | None = None, fly: bool = False):
         self.lib = load()
         self.bw = bw
         self.cutoff = bw if cutoff is None else cutoff
+        self.fly = fly
         h = C.c_void_p()
-        check(self.lib.s2g_plan_create(C.byref(h), bw, self.cutoff), "s2g_plan_create")
+        if fly:
+            check(self.lib.s2g_plan_create_fly(C.byref(h), bw), "s2g_plan_create_fly")
+        else:
+            check(self.lib.s2g_plan_create(C.byref(h), bw, self.cutoff), "s2g_plan_create")
         self.h = h
 
     def close(self):

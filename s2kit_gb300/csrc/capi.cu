@@ -299,14 +299,15 @@ static void report(const char* fn, int r) {
 // ---------------------------------------------------------------------------------
 // Drop-in implementations (return a status; the exported void wrappers print it).
 
+// fly: the on-the-fly family (no Legendre table on the device; `table` unused).
 static int do_fst(double* rdata, double* idata, double* rcoeffs, double* icoeffs, int bw, double** table,
-                  int fmt, int cutoff, double* weights) {
+                  int fmt, int cutoff, double* weights, bool fly = false) {
     S2G_TRY(check_bw(bw));
     S2G_TRY(check_cutoff(bw, cutoff));
     if (!rdata || !idata || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(dropin_device());
     Tables* base;
-    S2G_TRY(get_tables(bw, cutoff, &base));
+    S2G_TRY(get_tables(bw, fly ? 0 : cutoff, &base));
     TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
@@ -323,20 +324,23 @@ static int do_fst(double* rdata, double* idata, double* rcoeffs, double* icoeffs
         S2G_CUDA(cudaMemcpy(dw, weights, 4 * (size_t)bw * 8, cudaMemcpyHostToDevice));
         view.weights = dw;
     }
-    S2G_TRY(fst_f64(&view, dr, di, cr, ci, 1, fmt, cutoff, work, 0));
+    if (fly)
+        S2G_TRY(fst_f64_fly(&view, dr, di, cr, ci, 1, fmt, work, 0));
+    else
+        S2G_TRY(fst_f64(&view, dr, di, cr, ci, 1, fmt, cutoff, work, 0));
     S2G_CUDA(cudaMemcpy(rcoeffs, cr, nc * 8, cudaMemcpyDeviceToHost));
     S2G_CUDA(cudaMemcpy(icoeffs, ci, nc * 8, cudaMemcpyDeviceToHost));
     return S2G_OK;
 }
 
 static int do_inv_fst(double* rcoeffs, double* icoeffs, double* rdata, double* idata, int bw, double** ttable,
-                      int fmt, int cutoff) {
+                      int fmt, int cutoff, bool fly = false) {
     S2G_TRY(check_bw(bw));
     S2G_TRY(check_cutoff(bw, cutoff));
     if (!rdata || !idata || !rcoeffs || !icoeffs) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(dropin_device());
     Tables* base;
-    S2G_TRY(get_tables(bw, cutoff, &base));
+    S2G_TRY(get_tables(bw, fly ? 0 : cutoff, &base));
     TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
@@ -349,19 +353,22 @@ static int do_inv_fst(double* rcoeffs, double* icoeffs, double* rdata, double* i
     void* work = c.take(f64_work_bytes(bw, 1, fmt) / sizeof(double));
     S2G_CUDA(cudaMemcpy(cr, rcoeffs, nc * 8, cudaMemcpyHostToDevice));
     S2G_CUDA(cudaMemcpy(ci, icoeffs, nc * 8, cudaMemcpyHostToDevice));
-    S2G_TRY(inv_fst_f64(&view, cr, ci, dr, di, 1, fmt, cutoff, work, 0));
+    if (fly)
+        S2G_TRY(inv_fst_f64_fly(&view, cr, ci, dr, di, 1, fmt, work, 0));
+    else
+        S2G_TRY(inv_fst_f64(&view, cr, ci, dr, di, 1, fmt, cutoff, work, 0));
     S2G_CUDA(cudaMemcpy(rdata, dr, ng * 8, cudaMemcpyDeviceToHost));
     S2G_CUDA(cudaMemcpy(idata, di, ng * 8, cudaMemcpyDeviceToHost));
     return S2G_OK;
 }
 
 static int do_fzt(double* rdata, double* idata, double* rres, double* ires, int bw, double* cos_pml_table, int fmt,
-                  double* weights) {
+                  double* weights, bool fly = false) {
     S2G_TRY(check_bw(bw));
     if (!rdata || !idata || !rres || !ires) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(dropin_device());
     Tables* base;
-    S2G_TRY(get_tables(bw, bw, &base));
+    S2G_TRY(get_tables(bw, fly ? 0 : bw, &base));
     TabRef tref_{base};
     Tables view = *base;
     view.split = nullptr;
@@ -382,7 +389,10 @@ static int do_fzt(double* rdata, double* idata, double* rres, double* ires, int 
         S2G_CUDA(cudaMemcpy(dw, weights, 4 * (size_t)bw * 8, cudaMemcpyHostToDevice));
         view.weights = dw;
     }
-    S2G_TRY(fzt_f64(&view, dr, di, rr, ri, 1, fmt, work, 0));
+    if (fly)
+        S2G_TRY(fzt_f64_fly(&view, dr, di, rr, ri, 1, fmt, work, 0));
+    else
+        S2G_TRY(fzt_f64(&view, dr, di, rr, ri, 1, fmt, work, 0));
     S2G_CUDA(cudaMemcpy(rres, rr, (size_t)bw * 8, cudaMemcpyDeviceToHost));
     if (fmt == COMPLEX) {
         S2G_CUDA(cudaMemcpy(ires, ri, (size_t)bw * 8, cudaMemcpyDeviceToHost));
@@ -392,8 +402,10 @@ static int do_fzt(double* rdata, double* idata, double* rres, double* ires, int 
     return S2G_OK;
 }
 
+// t without Legendre tables (cutoff 0): the on-the-fly kernels.
 static int conv_device(const Tables* t, const double* dr, const double* di, const double* fr, const double* fi,
                        double* rr, double* ri, int batch, Scratch& scr, cudaStream_t st) {
+    const bool fly = (t->cutoff == 0);
     const int bw = t->bw;
     const size_t nc = (size_t)bw * bw;
     const size_t work = f64_work_bytes(bw, batch, REAL);
@@ -403,20 +415,28 @@ static int conv_device(const Tables* t, const double* dr, const double* di, cons
     double *cr = c.take(nc * batch), *ci = c.take(nc * batch), *tr = c.take(nc * batch), *ti = c.take(nc * batch);
     double *hr = c.take(2 * (size_t)bw * batch), *hi = c.take(2 * (size_t)bw * batch);
     void* w = c.take(work / sizeof(double));
-    S2G_TRY(fst_f64(t, dr, di, cr, ci, batch, REAL, bw, w, st));
-    S2G_TRY(fzt_f64(t, fr, fi, hr, hi, batch, REAL, w, st));
+    if (fly) {
+        S2G_TRY(fst_f64_fly(t, dr, di, cr, ci, batch, REAL, w, st));
+        S2G_TRY(fzt_f64_fly(t, fr, fi, hr, hi, batch, REAL, w, st));
+    } else {
+        S2G_TRY(fst_f64(t, dr, di, cr, ci, batch, REAL, bw, w, st));
+        S2G_TRY(fzt_f64(t, fr, fi, hr, hi, batch, REAL, w, st));
+    }
     S2G_TRY(transmult_f64(cr, ci, hr, hi, tr, ti, bw, batch, st));
-    S2G_TRY(inv_fst_f64(t, tr, ti, rr, ri, batch, REAL, bw, w, st));
+    if (fly)
+        S2G_TRY(inv_fst_f64_fly(t, tr, ti, rr, ri, batch, REAL, w, st));
+    else
+        S2G_TRY(inv_fst_f64(t, tr, ti, rr, ri, batch, REAL, bw, w, st));
     return S2G_OK;
 }
 
 static int do_conv(double* rdata, double* idata, double* rfilter, double* ifilter, double* rres, double* ires,
-                   int bw) {
+                   int bw, bool fly = false) {
     S2G_TRY(check_bw(bw));
     if (!rdata || !idata || !rfilter || !ifilter || !rres || !ires) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(dropin_device());
     Tables* t;
-    S2G_TRY(get_tables(bw, bw, &t));
+    S2G_TRY(get_tables(bw, fly ? 0 : bw, &t));
     TabRef tref_{t};
     const size_t S = 2 * (size_t)bw, ng = S * S;
     static thread_local DropinScratch io;
@@ -617,32 +637,33 @@ void ConvOn2SphereSemiMemo(double* rdata, double* idata, double* rfilter, double
     report("ConvOn2SphereSemiMemo", do_conv(rdata, idata, rfilter, ifilter, rres, ires, bw));
 }
 
-// On-the-fly family (src/FST_semi_fly.c): the reference generates each order's table inside the
-// call; here the tables are generated on the GPU for (bw, cutoff) on first use and kept for the
-// next call, so the transforms are those of the memo family on the device's own tables.
+// On-the-fly family (src/FST_semi_fly.c): like the reference, no Legendre table outlives an
+// order; here none is written at all, the recurrence runs inside the contraction kernels
+// (fst_f64_fly and companions).
 void FSTSemiFly(double* rdata, double* idata, double* rcoeffs, double* icoeffs, const int bw, double* workspace,
                 DataFormat data_format, const int cutoff, fftw_plan* DCT_plan, fftw_plan* FFT_plan,
                 double* weights) {
     (void)workspace; (void)DCT_plan; (void)FFT_plan;
-    report("FSTSemiFly", do_fst(rdata, idata, rcoeffs, icoeffs, bw, nullptr, (int)data_format, cutoff, weights));
+    report("FSTSemiFly",
+           do_fst(rdata, idata, rcoeffs, icoeffs, bw, nullptr, (int)data_format, cutoff, weights, true));
 }
 
 void InvFSTSemiFly(double* rcoeffs, double* icoeffs, double* rdata, double* idata, const int bw, double* workspace,
                    DataFormat data_format, const int cutoff, fftw_plan* inv_DCT_plan, fftw_plan* inv_FFT_plan) {
     (void)workspace; (void)inv_DCT_plan; (void)inv_FFT_plan;
-    report("InvFSTSemiFly", do_inv_fst(rcoeffs, icoeffs, rdata, idata, bw, nullptr, (int)data_format, cutoff));
+    report("InvFSTSemiFly", do_inv_fst(rcoeffs, icoeffs, rdata, idata, bw, nullptr, (int)data_format, cutoff, true));
 }
 
 void FZTSemiFly(double* rdata, double* idata, double* rres, double* ires, const int bw, double* workspace,
                 DataFormat data_format, fftw_plan* DCT_plan, double* weights) {
     (void)workspace; (void)DCT_plan;
-    report("FZTSemiFly", do_fzt(rdata, idata, rres, ires, bw, nullptr, (int)data_format, weights));
+    report("FZTSemiFly", do_fzt(rdata, idata, rres, ires, bw, nullptr, (int)data_format, weights, true));
 }
 
 void ConvOn2SphereSemiFly(double* rdata, double* idata, double* rfilter, double* ifilter, double* rres,
                           double* ires, const int bw, double* workspace) {
     (void)workspace;
-    report("ConvOn2SphereSemiFly", do_conv(rdata, idata, rfilter, ifilter, rres, ires, bw));
+    report("ConvOn2SphereSemiFly", do_conv(rdata, idata, rfilter, ifilter, rres, ires, bw, true));
 }
 
 void DLTSemi(double* data, const int bw, const int m, double* result, double* workspace, double* cos_pml_table,
@@ -890,6 +911,7 @@ struct HostDep {
 
 struct s2g_plan_s {
     int bw, cutoff, device;
+    bool fly = false;  // s2g_plan_create_fly: no Legendre table, on-the-fly kernels
     Tables* t;
     Scratch work;
     Scratch io;
@@ -976,6 +998,28 @@ int s2g_plan_create(s2g_plan* plan, int bw, int cutoff) {
     return S2G_OK;
 }
 
+int s2g_plan_create_fly(s2g_plan* plan, int bw) {
+    if (!plan) return fail(S2G_ERR_ARG, "NULL plan pointer");
+    *plan = nullptr;
+    S2G_TRY(check_bw(bw));
+    int dev;
+    S2G_TRY(current_device(&dev));
+    Tables* t;
+    S2G_TRY(get_tables(bw, 0, &t));
+    TabRef tref_{t};
+    s2g_plan p = new s2g_plan_s();
+    p->bw = bw;
+    p->cutoff = bw;
+    p->device = dev;
+    p->fly = true;
+    p->t = t;
+    for (auto& s : p->streams) S2G_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    for (auto& e : p->events) S2G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    tref_.t = nullptr;
+    *plan = p;
+    return S2G_OK;
+}
+
 int s2g_plan_destroy(s2g_plan p) {
     if (!p) return S2G_OK;
     cudaSetDevice(p->device);
@@ -1002,9 +1046,13 @@ size_t s2g_plan_workspace_size(s2g_plan p, int batch, int precision) {
 
 // Device-buffer calls share the plan's scratch with the host-buffer pipeline, so they first wait
 // for host-buffer work still queued (host = true: the pipeline itself, which orders its own work).
-static int plan_check(s2g_plan p, int batch, bool host = false) {
+// fly_ok: the entry point also runs on an on-the-fly plan (the FP64 transforms); the others need
+// the plan's Legendre tables.
+static int plan_check(s2g_plan p, int batch, bool host = false, bool fly_ok = false) {
     if (!p) return fail(S2G_ERR_ARG, "NULL plan");
     if (batch < 1) return fail(S2G_ERR_ARG, "batch %d < 1", batch);
+    if (p->fly && !fly_ok)
+        return fail(S2G_ERR_ARG, "an on-the-fly plan runs only s2g_fst, s2g_inv_fst, s2g_fzt and s2g_conv");
     int dev;
     S2G_TRY(current_device(&dev));
     if (dev != p->device) return fail(S2G_ERR_ARG, "plan made on device %d used on device %d", p->device, dev);
@@ -1014,26 +1062,30 @@ static int plan_check(s2g_plan p, int batch, bool host = false) {
 
 int s2g_fst(s2g_plan p, const double* rdata, const double* idata, double* rcoeffs, double* icoeffs, int batch,
             DataFormat fmt, void* stream) {
-    S2G_TRY(plan_check(p, batch));
+    S2G_TRY(plan_check(p, batch, false, true));
     if (!rdata || !rcoeffs || !icoeffs || (fmt == COMPLEX && !idata)) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(p->work.ensure(f64_work_bytes(p->bw, batch, fmt)));
+    if (p->fly) return fst_f64_fly(p->t, rdata, idata, rcoeffs, icoeffs, batch, fmt, p->work.ptr, (cudaStream_t)stream);
     return fst_f64(p->t, rdata, idata, rcoeffs, icoeffs, batch, fmt, p->cutoff, p->work.ptr, (cudaStream_t)stream);
 }
 
 int s2g_inv_fst(s2g_plan p, const double* rcoeffs, const double* icoeffs, double* rdata, double* idata, int batch,
                 DataFormat fmt, void* stream) {
-    S2G_TRY(plan_check(p, batch));
+    S2G_TRY(plan_check(p, batch, false, true));
     if (!rdata || !rcoeffs || !icoeffs || (fmt == COMPLEX && !idata)) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(p->work.ensure(f64_work_bytes(p->bw, batch, fmt)));
+    if (p->fly)
+        return inv_fst_f64_fly(p->t, rcoeffs, icoeffs, rdata, idata, batch, fmt, p->work.ptr, (cudaStream_t)stream);
     return inv_fst_f64(p->t, rcoeffs, icoeffs, rdata, idata, batch, fmt, p->cutoff, p->work.ptr,
                        (cudaStream_t)stream);
 }
 
 int s2g_fzt(s2g_plan p, const double* rdata, const double* idata, double* rres, double* ires, int batch,
             DataFormat fmt, void* stream) {
-    S2G_TRY(plan_check(p, batch));
+    S2G_TRY(plan_check(p, batch, false, true));
     if (!rdata || !rres || !ires || (fmt == COMPLEX && !idata)) return fail(S2G_ERR_ARG, "NULL argument");
     S2G_TRY(p->work.ensure(f64_work_bytes(p->bw, batch, REAL)));
+    if (p->fly) return fzt_f64_fly(p->t, rdata, idata, rres, ires, batch, fmt, p->work.ptr, (cudaStream_t)stream);
     return fzt_f64(p->t, rdata, idata, rres, ires, batch, fmt, p->work.ptr, (cudaStream_t)stream);
 }
 
@@ -1045,7 +1097,7 @@ int s2g_transmult(int bw, const double* rd, const double* id, const double* rf, 
 
 int s2g_conv(s2g_plan p, const double* rdata, const double* idata, const double* rfilter, const double* ifilter,
              double* rres, double* ires, int batch, void* stream) {
-    S2G_TRY(plan_check(p, batch));
+    S2G_TRY(plan_check(p, batch, false, true));
     if (p->cutoff != p->bw) return fail(S2G_ERR_ARG, "s2g_conv needs a plan with cutoff == bw");
     if (!rdata || !rfilter || !rres || !ires) return fail(S2G_ERR_ARG, "NULL argument");
     return conv_device(p->t, rdata, idata, rfilter, ifilter, rres, ires, batch, p->work, (cudaStream_t)stream);

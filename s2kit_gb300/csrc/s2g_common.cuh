@@ -226,6 +226,29 @@ __device__ inline void block_exclusive_scan(int* v, int n, int* warp_tot) {
 // ---------------------------------------------------------------------------------
 // Index helpers (device copies of the reference's integer formulas).
 
+// L2-normalised three-term recurrence P(m,l+1) = an(m,l) x P(m,l) + cn(m,l) P(m,l-1) and its seed
+// P(m,m)(cos theta) = pmm_const(m) sin(theta)^m.
+__device__ __forceinline__ double l2_an(int m, int l) {  // l2_norms.c:16-22
+    return sqrt(((2.0 * l + 3.0) / (2.0 * l + 1.0)) * ((l - m + 1.0) / (l + m + 1.0))) *
+           ((2.0 * l + 1.0) / (l - m + 1.0));
+}
+
+__device__ __forceinline__ double l2_cn(int m, int l) {  // l2_norms.c:28-38
+    if (l == 0) return 0.0;
+    return -sqrt(((2.0 * l + 3.0) / (2.0 * l - 1.0)) * ((l - m + 1.0) / (l + m + 1.0)) *
+                 (((double)l - m) / ((double)l + m))) *
+           ((l + m) / (l - m + 1.0));
+}
+
+// pmm.c:21-34 normalising constant (with the Condon-Shortley sign for odd m)
+__device__ inline double pmm_const(int m) {
+    double c = sqrt(m + 0.5);
+    for (int i = 0; i < m; ++i) c *= sqrt((m - (i / 2.0)) / ((double)m - i));
+    if (m) c *= exp2(-m / 2.0);
+    if (m % 2) c = -c;
+    return c;
+}
+
 // util.c:42-49
 __host__ __device__ __forceinline__ int index_of_harmonic_coeff(int m, int l, int bw) {
     const int L = bw - 1;

@@ -79,7 +79,8 @@ inline int check_aligned16(std::initializer_list<const void*> ps) {
 }
 
 // Build / fetch device tables (cached per device, bw, cutoff); the caller gets a reference and
-// returns it with put_tables.
+// returns it with put_tables.  cutoff 0 gives the weights, nodes and twiddles of bw without any
+// Legendre table (fwd, inv and off null), for the on-the-fly family.
 int get_tables(int bw, int cutoff, Tables** out);
 void put_tables(Tables* t);
 struct TabRef {
@@ -116,6 +117,15 @@ int fst_f64_len(const Tables* t, const Len* len_S, const double* rdata, const do
                 double* ic, int batch, int data_format, int cutoff, void* work, cudaStream_t st);
 int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rdata, double* idata, int batch,
                 int data_format, int cutoff, void* work, cudaStream_t st);
+// On-the-fly family (FST_semi_fly.c): the Legendre functions are generated inside the
+// contraction kernels, so `t` needs only its weights and twiddles (tables of cutoff 0, see
+// get_tables); work as f64_work_bytes.
+int fst_f64_fly(const Tables* t, const double* rdata, const double* idata, double* rc, double* ic, int batch,
+                int data_format, void* work, cudaStream_t st);
+int inv_fst_f64_fly(const Tables* t, const double* rc, const double* ic, double* rdata, double* idata, int batch,
+                    int data_format, void* work, cudaStream_t st);
+int fzt_f64_fly(const Tables* t, const double* rdata, const double* idata, double* rres, double* ires, int batch,
+                int data_format, void* work, cudaStream_t st);
 int fzt_f64(const Tables* t, const double* rdata, const double* idata, double* rres, double* ires, int batch,
             int data_format, void* work, cudaStream_t st);
 int transmult_f64(const double* rd, const double* id, const double* rf, const double* iff, double* rr,

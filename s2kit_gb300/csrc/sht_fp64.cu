@@ -573,6 +573,26 @@ static int launch_inv_dlt(InvDlt p, int nrows_grid, cudaStream_t st) {
     return S2G_OK;
 }
 
+// Inverse row DFT over the orders of each latitude: F [batch][rows][2B] -> samples.
+static int launch_rows_inv(const double* Fr, const double* Fi, int rows, int data_format, double* rdata,
+                           double* idata, int B, int batch, const double2* tw, cudaStream_t st) {
+    const int S = 2 * B;
+    Len L;
+    S2G_TRY(dft_len(S, &L));
+    const int R = rows_per_cta(S);
+    const int lat_per = idata ? R : 2 * R;
+    const size_t smem = rows_smem(L, R);
+    S2G_TRY(set_smem((const void*)k_rows_inv<double, double2>, smem));
+    dim3 grid((S + lat_per - 1) / lat_per, batch);
+    {
+        ProfScope ps_("rows_inv_f64", st);
+        k_rows_inv<double, double2><<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L, R,
+                                                              tw);
+    }
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
 size_t f64_work_bytes(int bw, int batch, int data_format) {
     const size_t S = 2 * (size_t)bw;
     const size_t rows = (data_format == COMPLEX) ? S : (size_t)bw;
@@ -638,19 +658,7 @@ int inv_fst_f64(const Tables* t, const double* rc, const double* ic, double* rda
     p.complex_rows = (data_format == COMPLEX);
     p.out_scale = 1.0 / sqrt(2.0 * kPi);  // FST_semi_memo.c:344-348
     S2G_TRY(launch_inv_dlt(p, (data_format == COMPLEX) ? S - 1 : B, st));
-    Len L;
-    S2G_TRY(dft_len(S, &L));
-    const int R = rows_per_cta(S);
-    const int lat_per = idata ? R : 2 * R;
-    const size_t smem = rows_smem(L, R);
-    S2G_TRY(set_smem((const void*)k_rows_inv<double, double2>, smem));
-    dim3 grid((S + lat_per - 1) / lat_per, batch);
-    {
-        ProfScope ps_("rows_inv_f64", st);
-        k_rows_inv<double, double2><<<grid, 256, smem, st>>>(Fr, Fi, rows, data_format == COMPLEX, rdata, idata, S, L, R, t->tw_S);
-    }
-    S2G_CUDA(cudaGetLastError());
-    return S2G_OK;
+    return launch_rows_inv(Fr, Fi, rows, data_format, rdata, idata, B, batch, t->tw_S, st);
 }
 
 int fzt_f64(const Tables* t, const double* rdata, const double* idata, double* rres, double* ires, int batch,
@@ -773,6 +781,379 @@ int inv_dlt_naive_f64(const double* coeffs, int bw, int m, double* result, const
     p.m1d = m;
     p.out_scale = 1.0;
     return launch_inv_dlt(p, 1, st);
+}
+
+// ------------------------------------------------------------------------------------
+// On-the-fly family (FST_semi_fly.c).  The reference builds every order's Legendre table inside
+// each call (GenerateCosPmlTable / GeneratePmlTable per order, FST_semi_fly.c:94-96, 257-261)
+// and keeps none of them.  Here no table is written at all: each thread runs the three-term
+// recurrence P(m,l) -> P(m,l+1) (pml.c:41-79: L2-normalised, seeded with P(m,m) of pmm.c:21-34)
+// at its own latitude nodes and contracts every value with the data as it is produced.  The
+// contraction is the reference's naive Legendre transform (DLTNaive / InvDLTNaive, naive.c:34-96,
+// which FST_semi_fly.c applies to the orders >= cutoff); in exact arithmetic it equals the
+// seminaive one that the reference applies below the cutoff, so every order runs naive here and
+// `cutoff` changes nothing but its validation.  Latitudes theta_j and pi - theta_j share
+// P(m,l) up to the sign (-1)^(l-m), so the data are folded into even and odd halves and only
+// the bw northern nodes carry a recurrence.  Device memory: the row-DFT workspace, no table.
+//
+// Forward: one CTA per (order row, G functions).  A tile of T = 16/G degrees gives each thread
+// T * 2G = 32 partial sums (degree x function x re/im) over its nodes; a warp reduce-scatter
+// leaves sum `lane` on each lane, and the warps' sums are added through shared memory.
+// Inverse: one thread per node and function group, summing a(l) P(m,l) over the degrees
+// (even and odd degrees apart, then unfolded), no reduction.
+
+constexpr int kFlyThreads = 256;
+constexpr int kFlyMaxPasses = 8;  // nodes per thread: bw <= 8 * 256
+
+struct FlyArgs {
+    const double* Xr;     // forward: row-DFT output [f][xrows][S]
+    const double* Xi;     // may be null (imaginary samples zero)
+    int xrows;
+    double* rc;           // forward: coefficients
+    double* ic;           // may be null
+    const double* crc;    // inverse: coefficients
+    const double* cic;    // may be null
+    int64_t c_stride;     // doubles between functions' coefficients
+    double* Fr;           // inverse: [f][frows][S] latitude vectors per order
+    double* Fi;           // may be null
+    int frows;
+    const double* w;      // forward: the 2B quadrature weights (weights.c:32-47)
+    int B, S, nfunc;
+    int complex_rows;     // rows 0..B-1 and B+1..S-1 (COMPLEX) else 0..B-1
+    int real_mirror;      // forward: fill f(l,-m) = (-1)^m conj f(l,m)
+    int one_d;            // order 0 from row 0, output result[l] (FZT)
+    double out_scale;     // inverse: FST_semi_memo.c:344-348
+};
+
+__device__ __forceinline__ void fly_row(const FlyArgs& p, int& row, int& m, bool& neg) {
+    neg = false;
+    if (p.one_d) {
+        row = 0;
+        m = 0;
+        return;
+    }
+    row = blockIdx.x;
+    if (p.complex_rows && row >= p.B) row += 1;
+    neg = row > p.B;
+    m = neg ? p.S - row : row;
+}
+
+template <int G>
+__global__ void __launch_bounds__(kFlyThreads) k_fly_fwd(FlyArgs p) {
+    constexpr int T = 16 / G;  // degrees per tile (even, so l - m = d mod 2 inside a tile)
+    constexpr int V = 2 * G;   // values per degree: function x (re, im)
+    extern __shared__ double sm[];
+    const int B = p.B, S = p.S;
+    int row, m;
+    bool neg;
+    fly_row(p, row, m, neg);
+    const double sgn = (neg && (row & 1)) ? -1.0 : 1.0;
+    const int f0 = blockIdx.y * G;
+    const int NT = blockDim.x, nw = NT >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double* sv = sm;                      // [B][2 parities][V] folded weighted data
+    double* an = sv + (size_t)B * 2 * V;  // [B] recurrence coefficients of this order
+    double* cn = an + B;
+    double* red = cn + B;                 // [nw][32]
+    __shared__ double cpmm;
+    if (threadIdx.x == 0) cpmm = (m == 0) ? 0.0 : pmm_const(m);
+    for (int l = m + threadIdx.x; l < B; l += NT) {
+        an[l] = l2_an(m, l);
+        cn[l] = l2_cn(m, l);
+    }
+    const int xrow = p.one_d ? 0 : row;
+    for (int i = threadIdx.x; i < B * G; i += NT) {
+        const int j = i % B, g = i / B, f = f0 + g;
+        double er = 0.0, ei = 0.0, orr = 0.0, oi = 0.0;
+        if (f < p.nfunc) {
+            const size_t base = ((size_t)f * p.xrows + xrow) * S;
+            const double wa = p.w[j], wb = p.w[S - 1 - j];
+            const double a = p.Xr[base + j] * wa, b = p.Xr[base + S - 1 - j] * wb;
+            er = a + b;
+            orr = a - b;
+            if (p.Xi) {
+                const double c = p.Xi[base + j] * wa, d = p.Xi[base + S - 1 - j] * wb;
+                ei = c + d;
+                oi = c - d;
+            }
+        }
+        double* q = sv + (size_t)j * 2 * V;
+        q[2 * g] = er;
+        q[2 * g + 1] = ei;
+        q[V + 2 * g] = orr;
+        q[V + 2 * g + 1] = oi;
+    }
+    __syncthreads();
+    // this thread's nodes j = threadIdx.x + r * NT: x = cos(theta_j), P(m,l) and P(m,l-1)
+    const int R = (B + NT - 1) / NT;
+    double x[kFlyMaxPasses], pc[kFlyMaxPasses], pp[kFlyMaxPasses];
+#pragma unroll
+    for (int r = 0; r < kFlyMaxPasses; ++r) {
+        x[r] = pc[r] = pp[r] = 0.0;
+        const int j = threadIdx.x + r * NT;
+        if (r < R && j < B) {
+            double sn, cs;
+            sincospi((2.0 * j + 1.0) / (2.0 * S), &sn, &cs);
+            x[r] = cs;
+            pc[r] = (m == 0) ? kSqrtHalf : cpmm * pow(sn, (double)m);
+        }
+    }
+    for (int l0 = m; l0 < B; l0 += T) {
+        double acc[T * V];
+#pragma unroll
+        for (int k = 0; k < T * V; ++k) acc[k] = 0.0;
+#pragma unroll
+        for (int r = 0; r < kFlyMaxPasses; ++r) {
+            const int j = threadIdx.x + r * NT;
+            if (r >= R || j >= B) continue;
+            const double* q = sv + (size_t)j * 2 * V;
+            double se[V], so[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                se[v] = q[v];
+                so[v] = q[V + v];
+            }
+#pragma unroll
+            for (int d = 0; d < T; ++d) {
+                const int l = l0 + d;
+                if (l >= B) break;
+                double val = pc[r];
+                if (l > m) {
+                    val = an[l - 1] * (pc[r] * x[r]) + cn[l - 1] * pp[r];
+                    pp[r] = pc[r];
+                    pc[r] = val;
+                }
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[d * V + v] = fma(val, (d & 1) ? so[v] : se[v], acc[d * V + v]);
+            }
+        }
+        // reduce-scatter over the warp: after the step of width h a lane keeps the half of its
+        // values whose index bit h equals its own lane bit, so lane L ends with value L
+#pragma unroll
+        for (int h = 16; h >= 1; h >>= 1) {
+            const bool up = (lane & h) != 0;
+#pragma unroll
+            for (int k = 0; k < h; ++k) {
+                const double send = up ? acc[k] : acc[k + h];
+                const double keep = up ? acc[k + h] : acc[k];
+                acc[k] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+            }
+        }
+        red[warp * 32 + lane] = acc[0];
+        __syncthreads();
+        if (warp == 0) {
+            double tot = 0.0;
+            for (int w2 = 0; w2 < nw; ++w2) tot += red[w2 * 32 + lane];
+            const int d = lane / V, v = lane % V, g = v >> 1, f = f0 + g;
+            const int l = l0 + d;
+            if (l < B && f < p.nfunc) {
+                const double val = sgn * tot;
+                if (p.one_d) {
+                    double* out = (v & 1) ? p.ic : p.rc;
+                    if (out) out[(size_t)f * p.c_stride + l] = val;
+                } else {
+                    const int idx = index_of_harmonic_coeff(neg ? -m : m, l, B);
+                    double* out = (v & 1) ? p.ic : p.rc;
+                    if (out) {
+                        out[(size_t)f * p.c_stride + idx] = val;
+                        if (p.real_mirror && m > 0) {
+                            // f(l,-m) = (-1)^m conj f(l,m)   (FST_semi_memo.c:131-145)
+                            const double sm_ = (m & 1) ? -1.0 : 1.0;
+                            out[(size_t)f * p.c_stride + index_of_harmonic_coeff(-m, l, B)] =
+                                (v & 1) ? -sm_ * val : sm_ * val;
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(kFlyThreads) k_fly_inv(FlyArgs p) {
+    constexpr int V = 2 * G;
+    extern __shared__ double sm[];
+    const int B = p.B, S = p.S;
+    int row, m;
+    bool neg;
+    fly_row(p, row, m, neg);
+    const double sgn = ((neg && (row & 1)) ? -1.0 : 1.0) * p.out_scale;
+    const int f0 = blockIdx.y * G;
+    const int NT = blockDim.x;
+    const int nl = B - m;
+    double* a = sm;                    // [nl][V] coefficients of this order
+    double* an = a + (size_t)B * V;    // [B]
+    double* cn = an + B;
+    __shared__ double cpmm;
+    if (threadIdx.x == 0) cpmm = (m == 0) ? 0.0 : pmm_const(m);
+    for (int l = m + threadIdx.x; l < B; l += NT) {
+        an[l] = l2_an(m, l);
+        cn[l] = l2_cn(m, l);
+    }
+    for (int i = threadIdx.x; i < nl * G; i += NT) {
+        const int li = i % nl, g = i / nl, f = f0 + g;
+        double vr = 0.0, vi = 0.0;
+        if (f < p.nfunc) {
+            const int idx = p.one_d ? li : index_of_harmonic_coeff(neg ? -m : m, m + li, B);
+            vr = p.crc[(size_t)f * p.c_stride + idx];
+            vi = p.cic ? p.cic[(size_t)f * p.c_stride + idx] : 0.0;
+        }
+        a[(size_t)li * V + 2 * g] = vr;
+        a[(size_t)li * V + 2 * g + 1] = vi;
+    }
+    __syncthreads();
+    const int frow = p.one_d ? 0 : row;
+    for (int j = threadIdx.x; j < B; j += NT) {
+        double sn, x;
+        sincospi((2.0 * j + 1.0) / (2.0 * S), &sn, &x);
+        double pc = (m == 0) ? kSqrtHalf : cpmm * pow(sn, (double)m);
+        double pp = 0.0;
+        double ev[V], od[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) ev[v] = od[v] = 0.0;
+        // degrees in pairs: l - m even into ev, odd into od
+        for (int l = m; l < B; l += 2) {
+            const double* al = a + (size_t)(l - m) * V;
+#pragma unroll
+            for (int v = 0; v < V; ++v) ev[v] = fma(pc, al[v], ev[v]);
+            if (l + 1 >= B) break;
+            double nx = an[l] * (pc * x) + cn[l] * pp;
+            pp = pc;
+            pc = nx;
+#pragma unroll
+            for (int v = 0; v < V; ++v) od[v] = fma(pc, al[V + v], od[v]);
+            if (l + 2 >= B) break;
+            nx = an[l + 1] * (pc * x) + cn[l + 1] * pp;
+            pp = pc;
+            pc = nx;
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int f = f0 + g;
+            if (f >= p.nfunc) break;
+            const size_t o = ((size_t)f * p.frows + frow) * S;
+            p.Fr[o + j] = sgn * (ev[2 * g] + od[2 * g]);
+            p.Fr[o + S - 1 - j] = sgn * (ev[2 * g] - od[2 * g]);
+            if (p.Fi) {
+                p.Fi[o + j] = sgn * (ev[2 * g + 1] + od[2 * g + 1]);
+                p.Fi[o + S - 1 - j] = sgn * (ev[2 * g + 1] - od[2 * g + 1]);
+            }
+        }
+    }
+}
+
+static size_t fly_fwd_smem(int B, int G) {
+    return ((size_t)B * 4 * G + 2 * (size_t)B + (kFlyThreads / 32) * 32) * sizeof(double);
+}
+static size_t fly_inv_smem(int B, int G) { return ((size_t)B * 2 * G + 2 * (size_t)B) * sizeof(double); }
+
+// Functions per CTA: as many (up to 4) as the batch has, within 200 KiB of shared memory.
+template <typename SmemFn>
+static int fly_group(int B, int nfunc, SmemFn smem) {
+    int G = nfunc >= 4 ? 4 : (nfunc >= 2 ? 2 : 1);
+    while (G > 1 && smem(B, G) > 200 * 1024) G /= 2;
+    return G;
+}
+
+static int launch_fly(bool fwd, FlyArgs p, int nrows, cudaStream_t st) {
+    if (p.B > kFlyMaxPasses * kFlyThreads)
+        return fail(S2G_ERR_UNSUPPORTED, "bandwidth %d too large for the on-the-fly kernels", p.B);
+    const int G = fwd ? fly_group(p.B, p.nfunc, fly_fwd_smem) : fly_group(p.B, p.nfunc, fly_inv_smem);
+    const size_t smem = fwd ? fly_fwd_smem(p.B, G) : fly_inv_smem(p.B, G);
+    const int nt = p.B >= kFlyThreads ? kFlyThreads : ((p.B + 31) / 32) * 32;
+    dim3 grid(nrows, (p.nfunc + G - 1) / G);
+    const void* fn = fwd ? (G == 4 ? (const void*)k_fly_fwd<4> : G == 2 ? (const void*)k_fly_fwd<2>
+                                                                        : (const void*)k_fly_fwd<1>)
+                         : (G == 4 ? (const void*)k_fly_inv<4> : G == 2 ? (const void*)k_fly_inv<2>
+                                                                        : (const void*)k_fly_inv<1>);
+    S2G_TRY(set_smem(fn, smem));
+    {
+        ProfScope ps_(fwd ? "fly_fwd_f64" : "fly_inv_f64", st);
+        if (fwd) {
+            if (G == 4) k_fly_fwd<4><<<grid, nt, smem, st>>>(p);
+            else if (G == 2) k_fly_fwd<2><<<grid, nt, smem, st>>>(p);
+            else k_fly_fwd<1><<<grid, nt, smem, st>>>(p);
+        } else {
+            if (G == 4) k_fly_inv<4><<<grid, nt, smem, st>>>(p);
+            else if (G == 2) k_fly_inv<2><<<grid, nt, smem, st>>>(p);
+            else k_fly_inv<1><<<grid, nt, smem, st>>>(p);
+        }
+    }
+    S2G_CUDA(cudaGetLastError());
+    return S2G_OK;
+}
+
+int fst_f64_fly(const Tables* t, const double* rdata, const double* idata, double* rc, double* ic, int batch,
+                int data_format, void* work, cudaStream_t st) {
+    const int B = t->bw, S = 2 * B;
+    const int rows = (data_format == COMPLEX) ? S : B;
+    double* Xr = (double*)work;
+    double* Xi = Xr + (size_t)batch * rows * S;
+    S2G_TRY(launch_rows_fwd(rdata, idata, Xr, Xi, B, rows, batch, t->tw_S, st));
+    FlyArgs p{};
+    p.Xr = Xr;
+    p.Xi = Xi;
+    p.xrows = rows;
+    p.rc = rc;
+    p.ic = ic;
+    p.c_stride = (int64_t)B * B;
+    p.w = t->weights;
+    p.B = B;
+    p.S = S;
+    p.nfunc = batch;
+    p.complex_rows = (data_format == COMPLEX);
+    p.real_mirror = (data_format != COMPLEX);
+    return launch_fly(true, p, (data_format == COMPLEX) ? S - 1 : B, st);
+}
+
+int inv_fst_f64_fly(const Tables* t, const double* rc, const double* ic, double* rdata, double* idata, int batch,
+                    int data_format, void* work, cudaStream_t st) {
+    const int B = t->bw, S = 2 * B;
+    const int rows = (data_format == COMPLEX) ? S : B;
+    double* Fr = (double*)work;
+    double* Fi = Fr + (size_t)batch * rows * S;
+    FlyArgs p{};
+    p.crc = rc;
+    p.cic = ic;
+    p.c_stride = (int64_t)B * B;
+    p.Fr = Fr;
+    p.Fi = Fi;
+    p.frows = rows;
+    p.B = B;
+    p.S = S;
+    p.nfunc = batch;
+    p.complex_rows = (data_format == COMPLEX);
+    p.out_scale = 1.0 / sqrt(2.0 * kPi);  // FST_semi_memo.c:344-348
+    S2G_TRY(launch_fly(false, p, (data_format == COMPLEX) ? S - 1 : B, st));
+    return launch_rows_inv(Fr, Fi, rows, data_format, rdata, idata, B, batch, t->tw_S, st);
+}
+
+int fzt_f64_fly(const Tables* t, const double* rdata, const double* idata, double* rres, double* ires, int batch,
+                int data_format, void* work, cudaStream_t st) {
+    const int B = t->bw, S = 2 * B;
+    double* Xr = (double*)work;
+    double* Xi = Xr + (size_t)batch * S;
+    dim3 g1((S + 7) / 8, batch);
+    {
+        ProfScope ps_("rowsum_f64", st);
+        k_rowsum<<<g1, 256, 0, st>>>(rdata, idata, Xr, Xi, S, sqrt(2.0 * kPi) / S);
+    }
+    S2G_CUDA(cudaGetLastError());
+    FlyArgs p{};
+    p.Xr = Xr;
+    p.Xi = (data_format == COMPLEX) ? Xi : nullptr;
+    p.xrows = 1;
+    p.rc = rres;
+    p.ic = (data_format == COMPLEX) ? ires : nullptr;
+    p.c_stride = B;
+    p.w = t->weights;
+    p.B = B;
+    p.S = S;
+    p.nfunc = batch;
+    p.one_d = 1;
+    S2G_TRY(launch_fly(true, p, 1, st));
+    if (data_format != COMPLEX) S2G_CUDA(cudaMemsetAsync(ires, 0, sizeof(double) * (size_t)batch * B, st));
+    return S2G_OK;
 }
 
 }  // namespace s2g

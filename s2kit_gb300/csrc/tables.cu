@@ -21,27 +21,6 @@ namespace s2g {
 
 static constexpr double kSqrtHalf = 0.70710678118654752440;
 
-__device__ __forceinline__ double l2_an(int m, int l) {  // l2_norms.c:16-22
-    return sqrt(((2.0 * l + 3.0) / (2.0 * l + 1.0)) * ((l - m + 1.0) / (l + m + 1.0))) *
-           ((2.0 * l + 1.0) / (l - m + 1.0));
-}
-
-__device__ __forceinline__ double l2_cn(int m, int l) {  // l2_norms.c:28-38
-    if (l == 0) return 0.0;
-    return -sqrt(((2.0 * l + 3.0) / (2.0 * l - 1.0)) * ((l - m + 1.0) / (l + m + 1.0)) *
-                 (((double)l - m) / ((double)l + m))) *
-           ((l + m) / (l - m + 1.0));
-}
-
-// pmm.c:21-34 normalising constant (with the Condon-Shortley sign for odd m)
-__device__ double pmm_const(int m) {
-    double c = sqrt(m + 0.5);
-    for (int i = 0; i < m; ++i) c *= sqrt((m - (i / 2.0)) / ((double)m - i));
-    if (m) c *= exp2(-m / 2.0);
-    if (m % 2) c = -c;
-    return c;
-}
-
 struct GenCos {
     int B;
     int m0;
@@ -322,6 +301,18 @@ static void host_offsets(int bw, int cutoff, std::vector<int64_t>& off, int64_t*
 
 int build_tables(Tables* t, cudaStream_t st, const double* h_fwd, const double* h_inv) {
     const int B = t->bw, S = 2 * B;
+    S2G_CUDA(cudaMalloc(&t->weights, sizeof(double) * 4 * B));
+    S2G_CUDA(cudaMalloc(&t->sinv, sizeof(double) * S));
+    S2G_CUDA(cudaMalloc(&t->tw_S, sizeof(double2) * S));
+    S2G_CUDA(cudaMalloc(&t->tw_D, sizeof(double2) * S));
+    S2G_TRY(generate_weights_device(B, t->weights, st));
+    S2G_TRY(nodes_device(S, t->sinv, 2, st));
+    S2G_TRY(twiddles_device(S, t->tw_S, t->tw_D, st));
+    if (t->cutoff == 0) {  // on-the-fly family: no Legendre table
+        t->total = 0;
+        S2G_CUDA(cudaStreamSynchronize(st));
+        return S2G_OK;
+    }
     std::vector<int64_t> off;
     host_offsets(B, t->cutoff, off, &t->total);
     t->h_off = new int64_t[B];
@@ -329,14 +320,7 @@ int build_tables(Tables* t, cudaStream_t st, const double* h_fwd, const double* 
     S2G_CUDA(cudaMalloc(&t->fwd, sizeof(double) * (size_t)(t->total > 0 ? t->total : 1)));
     S2G_CUDA(cudaMalloc(&t->inv, sizeof(double) * (size_t)(t->total > 0 ? t->total : 1)));
     S2G_CUDA(cudaMalloc(&t->off, sizeof(int64_t) * B));
-    S2G_CUDA(cudaMalloc(&t->weights, sizeof(double) * 4 * B));
-    S2G_CUDA(cudaMalloc(&t->sinv, sizeof(double) * S));
-    S2G_CUDA(cudaMalloc(&t->tw_S, sizeof(double2) * S));
-    S2G_CUDA(cudaMalloc(&t->tw_D, sizeof(double2) * S));
     S2G_CUDA(cudaMemcpyAsync(t->off, off.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice, st));
-    S2G_TRY(generate_weights_device(B, t->weights, st));
-    S2G_TRY(nodes_device(S, t->sinv, 2, st));
-    S2G_TRY(twiddles_device(S, t->tw_S, t->tw_D, st));
     const int cut = t->cutoff;
     if (h_fwd && h_inv) {
         S2G_CUDA(cudaMemcpyAsync(t->fwd, h_fwd, sizeof(double) * (size_t)t->total, cudaMemcpyHostToDevice, st));

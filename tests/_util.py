@@ -59,3 +59,39 @@ def rel_err_norm(got_r, got_i, ref_r, ref_i):
 
 def max_abs(a, b):
     return float(np.max(np.abs(np.asarray(a) - np.asarray(b))))
+
+
+def block_norms(v, block):
+    """L2 norm of every consecutive block of `block` values (the last one zero-padded)."""
+    v = np.asarray(v, dtype=np.float64)
+    v = np.pad(v, (0, -v.size % block))
+    return np.sqrt((v.reshape(-1, block) ** 2).sum(axis=1))
+
+
+def bw1024_inputs(g):
+    """The seeded inputs of tests/golden/ref_bw1024.npz (a real field with coefficients
+    N(0,1)(1+l)^-1, a noise grid, the zonal filter exp(-l(l+1)/(2*150^2))), regenerated and
+    checked against the fixture's checksums."""
+    bw = 1024
+    rc, ic = real_field_coeffs(np.random.default_rng(1024), bw, 1.0)
+    noise = np.random.default_rng(1025).standard_normal(4 * bw * bw)
+    assert rc.sum() == g["rc_sum"] and ic.sum() == g["ic_sum"] and (rc ** 2).sum() == g["rc_sq"]
+    assert noise.sum() == g["noise_sum"]
+    l = np.arange(bw)
+    hr = np.zeros(bw * bw)
+    hr[harmonic_index(0, l, bw)] = np.exp(-l * (l + 1) / (2 * 150.0 ** 2))
+    return rc, ic, noise, hr
+
+
+def vs_sampled_reference(g, name, got_r, got_i, tol):
+    """One full output (grid or coefficients) against the reference's values at the fixture's
+    sample positions and its block norms; returns the larger normwise error."""
+    bw = int(g["bw"])
+    pos = g["grid_pos"] if np.asarray(got_r).size == 4 * bw * bw else g["coef_pos"]
+    e_s = rel_err_norm(got_r[pos], got_i[pos], g[f"{name}_r"], g[f"{name}_i"])
+    blk = int(g["block"])
+    scale = max(g[f"{name}_r_blocks"].max(), g[f"{name}_i_blocks"].max())
+    e_b = max(np.abs(block_norms(got_r, blk) - g[f"{name}_r_blocks"]).max(),
+              np.abs(block_norms(got_i, blk) - g[f"{name}_i_blocks"]).max()) / scale
+    assert e_s <= tol and e_b <= tol, (name, e_s, e_b)
+    return max(e_s, e_b)

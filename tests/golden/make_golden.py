@@ -1,9 +1,8 @@
 """Generate the committed golden fixtures in tests/golden/ from the S2kit reference.
 
-Run in a container that has the reference checkout (default /root/reference, or
-$S2_REFERENCE_DIR):
+Run where the reference checkout exists, naming it with $S2_REFERENCE_DIR:
 
-    python tests/golden/make_golden.py
+    S2_REFERENCE_DIR=<S2kit checkout> python tests/golden/make_golden.py [--only bw1024]
 
 Two kinds of fixture are written (all float64, np.savez_compressed):
 
@@ -18,6 +17,13 @@ Two kinds of fixture are written (all float64, np.savez_compressed):
   (FSTSemiMemo, InvFSTSemiMemo, FZTSemiMemo, ConvOn2SphereSemiMemo, DLTSemi/InvDLTSemi,
   table generators, GenerateWeightsForDLT) on seeded inputs -> ref_*.npz, and of the
   on-the-fly family (FSTSemiFly, InvFSTSemiFly, FZTSemiFly, ConvOn2SphereSemiFly) -> ref_fly.npz.
+* the large single-function workload at bw 1024 (ref_bw1024.npz): the reference's tables,
+  InvFSTSemiMemo / FSTSemiMemo of a seeded real field (N(0,1)(1+l)^-1), FSTSemiMemo of seeded
+  noise and ConvOn2SphereSemiMemo with the zonal filter exp(-l(l+1)/(2*150^2)).  The full
+  outputs (16-32 MiB each) are too large to commit, so the fixture holds, for each output, the
+  values at a seeded sample of positions (some in every order for the tables) and the L2 norm of
+  every consecutive block of 4096 values (65536 for the tables); the inputs are regenerated from their seeds by the
+  tests and checked against stored checksums.
 """
 from __future__ import annotations
 
@@ -31,7 +37,13 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from oracle.oracle import COMPLEX, REAL, Reference  # noqa: E402
 
-REF = os.environ.get("S2_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("S2_REFERENCE_DIR", "")
+
+# sample sizes of the bw-1024 fixture
+BW1024 = 1024
+SAMPLE = 4096
+BLOCK = 4096          # outputs (grids: 1024 blocks, coefficients: 256)
+TABLE_BLOCK = 65536   # tables (2735 blocks each)
 
 
 def real_field_coeffs(rng, bw, p=0.0):
@@ -54,9 +66,74 @@ def real_field_coeffs(rng, bw, p=0.0):
     return rc, ic
 
 
+def block_norms(v, block=BLOCK):
+    """L2 norm of every consecutive block of `block` values (the last one zero-padded)."""
+    v = np.asarray(v, dtype=np.float64)
+    v = np.pad(v, (0, -v.size % block))
+    return np.sqrt((v.reshape(-1, block) ** 2).sum(axis=1))
+
+
+def bw1024_inputs():
+    """The seeded inputs of ref_bw1024.npz: coefficients of a real field N(0,1)(1+l)^-1, a noise
+    grid, the zonal filter's coefficients, and the sample positions.  tests/ regenerate them."""
+    from tests._util import harmonic_index, real_field_coeffs
+    bw = BW1024
+    rc, ic = real_field_coeffs(np.random.default_rng(1024), bw, 1.0)
+    noise = np.random.default_rng(1025).standard_normal(4 * bw * bw)
+    l = np.arange(bw)
+    hr = np.zeros(bw * bw)
+    hr[harmonic_index(0, l, bw)] = np.exp(-l * (l + 1) / (2 * 150.0 ** 2))
+    ps = np.random.default_rng(1026)
+    return dict(rc=rc, ic=ic, noise=noise, filter_r=hr, coef_pos=np.sort(ps.choice(bw * bw, SAMPLE, replace=False)),
+                grid_pos=np.sort(ps.choice(4 * bw * bw, SAMPLE, replace=False)))
+
+
+def bw1024_table_positions(offsets, total, bw):
+    """Sample positions in the packed tables: up to 8 entries of every order plus SAMPLE more."""
+    ps = np.random.default_rng(1027)
+    ends = np.append(offsets[1:], total)
+    pos = [np.sort(ps.choice(np.arange(a, b), min(8, b - a), replace=False)) for a, b in zip(offsets, ends)]
+    pos.append(ps.choice(total, SAMPLE, replace=False))
+    return np.unique(np.concatenate(pos))
+
+
+def make_bw1024(r, out):
+    bw = BW1024
+    x = bw1024_inputs()
+    tf, ti, fwd, inv = r.tables(bw, bw)
+    size = fwd.size
+    # order offsets of the packed table (m < cutoff = bw: cosine tables back to back)
+    offsets = np.cumsum([0] + [r.lib.TableSize(m, bw) for m in range(bw - 1)]).astype(np.int64)
+    tpos = bw1024_table_positions(offsets, size, bw)
+    grid_r, grid_i = r.inv_fst(x["rc"], x["ic"], bw, REAL, bw, tables=(tf, ti, fwd, inv))
+    rt_r, rt_i = r.fst(grid_r, grid_i, bw, REAL, bw, tables=(tf, ti, fwd, inv))
+    nz = np.zeros(4 * bw * bw)
+    nf_r, nf_i = r.fst(x["noise"], nz, bw, REAL, bw, tables=(tf, ti, fwd, inv))
+    filt_r, _ = r.inv_fst(x["filter_r"], np.zeros(bw * bw), bw, REAL, bw, tables=(tf, ti, fwd, inv))
+    cv_r, cv_i = r.conv(grid_r, nz, filt_r, nz, bw)
+    cp, gp = x["coef_pos"], x["grid_pos"]
+    res = dict(bw=bw, block=BLOCK, table_block=TABLE_BLOCK, rc_sum=x["rc"].sum(), ic_sum=x["ic"].sum(),
+               rc_sq=(x["rc"] ** 2).sum(), noise_sum=x["noise"].sum(), coef_pos=cp, grid_pos=gp, table_pos=tpos,
+               table_offsets=offsets, table_fwd=fwd[tpos], table_inv=inv[tpos],
+               table_fwd_blocks=block_norms(fwd, TABLE_BLOCK), table_inv_blocks=block_norms(inv, TABLE_BLOCK))
+    for name, (a, b) in dict(inv=(grid_r, grid_i), rt=(rt_r, rt_i), noise_fwd=(nf_r, nf_i), filter_grid=(filt_r, nz),
+                             conv=(cv_r, cv_i)).items():
+        pos = gp if a.size == 4 * bw * bw else cp
+        res[f"{name}_r"], res[f"{name}_i"] = a[pos], b[pos]
+        res[f"{name}_r_blocks"], res[f"{name}_i_blocks"] = block_norms(a), block_norms(b)
+    np.savez_compressed(os.path.join(out, "ref_bw1024.npz"), **res)
+
+
 def main():
-    r = Reference()
+    if not os.path.isdir(os.path.join(REF, "src")):
+        raise SystemExit("set S2_REFERENCE_DIR to the S2kit checkout")
+    r = Reference(REF)
     out = HERE
+    if "--only" in sys.argv:
+        if sys.argv[sys.argv.index("--only") + 1] == "bw1024":
+            make_bw1024(r, out)
+            return
+        raise SystemExit("--only takes: bw1024")
 
     # ---- copied reference data --------------------------------------------------------
     for bw in (64, 128):
@@ -154,6 +231,7 @@ def main():
     fly["conv_bw16_out_r"], fly["conv_bw16_out_i"] = r.conv_fly(sig, np.zeros(4 * bw * bw), filt_r,
                                                                 np.zeros(4 * bw * bw), bw)
     np.savez_compressed(os.path.join(out, "ref_fly.npz"), **fly)
+    make_bw1024(r, out)
 
     print("fixtures written to", out)
 

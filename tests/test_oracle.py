@@ -178,3 +178,32 @@ def test_oracle_matches_reference_fly_fzt_conv(oracle, golden):
     z = np.zeros(4 * 16 * 16)
     cr, ci = oracle.conv(g["conv_bw16_signal"], z, g["conv_bw16_filter"], z, 16)
     assert rel_err_norm(cr, ci, g["conv_bw16_out_r"], g["conv_bw16_out_i"]) <= 1e-14
+
+
+def test_oracle_matches_reference_at_bw1024(oracle, golden):
+    """The large single-function workload (bw 1024): the oracle's tables, inverse and forward
+    transforms, forward of noise and convolution with the zonal filter exp(-l(l+1)/(2*150^2))
+    against the reference's own outputs (sampled values and block norms, ref_bw1024.npz)."""
+    from tests._util import block_norms, bw1024_inputs, vs_sampled_reference
+    g = golden("ref_bw1024")
+    bw = int(g["bw"])
+    rc, ic, noise, hr = bw1024_inputs(g)
+    try:
+        _, fwd, inv, off = oracle.tables(bw, bw)
+        assert np.array_equal(off, g["table_offsets"])
+        pos = g["table_pos"]
+        scale = np.abs(fwd).max()
+        assert np.abs(fwd[pos] - g["table_fwd"]).max() <= 1e-13 * scale
+        assert np.abs(inv[pos] - g["table_inv"]).max() <= 1e-13 * scale
+        tb = int(g["table_block"])
+        assert np.abs(block_norms(fwd, tb) - g["table_fwd_blocks"]).max() <= 1e-13 * g["table_fwd_blocks"].max()
+        assert np.abs(block_norms(inv, tb) - g["table_inv_blocks"]).max() <= 1e-13 * g["table_inv_blocks"].max()
+        z = np.zeros(4 * bw * bw)
+        grid, _ = oracle.inv_fst(rc, ic, bw, REAL, bw)
+        filt, _ = oracle.inv_fst(hr, np.zeros(bw * bw), bw, REAL, bw)
+        outs = {"inv": (grid, z), "rt": oracle.fst(grid, z, bw, REAL, bw), "noise_fwd": oracle.fst(noise, z, bw, REAL, bw),
+                "filter_grid": (filt, z), "conv": oracle.conv(grid, z, filt, z, bw, cached_tables=True)}
+        for name, (a, b) in outs.items():
+            vs_sampled_reference(g, name, a, b, tol=1e-13)
+    finally:
+        oracle.drop_tables(bw, bw)
