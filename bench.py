@@ -590,15 +590,36 @@ def large_bw1024_bench(api, torch, stream, seed):
     mag = torch.hypot(f_r, f_i).amax(dim=1)
     e_split = (torch.hypot(s_r.double() - f_r, s_i.double() - f_i).amax(dim=1) / mag).max().item()
     e_ref = (torch.hypot(r_r - f_r, r_i - f_i).amax(dim=1) / mag).max().item()
+    # the on-the-fly family (no Legendre table on the device): FP64 fwd+inv of the same functions
+    y_g = torch.empty_like(g64)
+    y_r, y_i = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    fly = api.Plan(B, fly=True)
+
+    def step_fly():
+        fly.inv_fst(d_rc, d_ic, y_g, None, N, api.REAL, stream)
+        fly.fst(y_g, None, y_r, y_i, N, api.REAL, stream)
+
+    msf = _time(torch, stream, step_fly, 3)
+    fly_mib = (free0 - torch.cuda.mem_get_info()[0]) / 2 ** 20
+    e_fly = max((torch.hypot(y_r - f_r, y_i - f_i).amax(dim=1) / mag).max().item(),
+                ((y_g - g64).abs().amax(dim=1) / g64.abs().amax(dim=1)).max().item())
+    fly.close()
     return {"workload": "16 real functions at bw 1024, (1+l)^-1", "split_bf16x3_fwd_inv_per_s": N / (ms32 / 1e3),
             "fp64_fwd_inv_per_s": N / (ms64 / 1e3), "refined_fwd_per_s": N / (msr / 1e3),
-            "split_fwd_err_vs_fp64": e_split, "refined_fwd_err_vs_fp64": e_ref}
+            "split_fwd_err_vs_fp64": e_split, "refined_fwd_err_vs_fp64": e_ref,
+            "fly_fp64_fwd_inv_per_s": N / (msf / 1e3), "fly_device_mib": fly_mib, "fly_err_vs_memo_fp64": e_fly,
+            "fly_note": "on-the-fly plan: Legendre recurrence inside the contraction kernels, no table "
+                        "(the memo tables of bw 1024 take 2 x 1.37 GiB); its device memory is the row-DFT "
+                        "workspace of the 16 functions (2 x 1024 x 2048 doubles each)"}
 
 
 def group_bench(api, torch, stream, steps, warmup, seed):
     """Grouped uneven-bandwidth workload: 512 real functions, bandwidths {16..256} with
     probabilities {.3,.3,.2,.15,.05}, coefficients N(0,1)(1+l)^-2, split FP16, forward+inverse
-    as one replayed CUDA graph (one persistent contraction launch per direction), autotuned tiles.
+    as one replayed CUDA graph (per direction: each FFT stage one grouped launch per tier of
+    classes, the tiers concurrent, and one persistent contraction launch), autotuned shapes.
     Returns fwd+inv functions/s and the per-bandwidth error vs the FP64 path."""
     rng = np.random.default_rng(seed)
     bws = rng.choice([16, 32, 64, 128, 256], size=512, p=[0.3, 0.3, 0.2, 0.15, 0.05]).tolist()
@@ -650,10 +671,25 @@ def group_bench(api, torch, stream, steps, warmup, seed):
         e_rt = ((s_g - g64).abs().amax(dim=1) / g64.abs().amax(dim=1)).max().item()
         errs[str(B)] = {"functions": len(idx), "coeff_err": e_f, "roundtrip_grid_err": e_rt}
     d = g.describe()
+    # per-stage event timing: eager runs of the same sequence (re-applying the shapes drops the graph)
+    import ctypes
+    lib = api.load()
+    t = d["tiles"]
+    tiles = [t["tile_n"][str(c[0])] for c in d["classes"]]
+    lib.s2g_prof_enable(1)
+    for _ in range(5):
+        g.set_tiles(t["ctas_per_sm"], tiles, t["dct_ctas_per_sm"])
+        g.fst_inv(grid, o_rc, o_ic, o_grid, stream)
+    torch.cuda.synchronize()
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib.s2g_prof_report(buf, len(buf))
+    lib.s2g_prof_enable(0)
+    stages = {k: v[1] / v[0] for k, v in json.loads(buf.value.decode()).items()}
     return {"workload": "512 real functions, bw in {16,32,64,128,256} w.p. {.3,.3,.2,.15,.05}, (1+l)^-2, "
                         "split FP16, fwd+inv as one CUDA graph", "value": 512 / (ms / 1e3),
             "unit": "fwd+inv functions/s", "ms_per_step": ms, "steps": k, "tiles": d["tiles"],
-            "graph_kernels": d["graph_kernels"][2], "autotune_s": tune_s, "per_bw": errs}
+            "graph_kernels": d["graph_kernels"][2], "stage_ms_eager": stages, "autotune_s": tune_s,
+            "per_bw": errs}
 
 
 def tc_flops_issued(B, N, fwd, nprod):

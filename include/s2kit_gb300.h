@@ -292,11 +292,12 @@ int s2g_plan_sync_status(s2g_plan plan);
  * on the device: the functions back to back in the order given, function f's grid taking
  * (2 bw[f])^2 floats and its coefficients bw[f]^2 floats in each of rcoeffs/icoeffs (the
  * reference layout per function, negative orders written by symmetry as s2g_fst_real_f32);
- * s2g_group_layout returns the offsets.  A call runs the phi-FFT/DCT stages of each bandwidth
- * class concurrently and ONE persistent tensor-core contraction launch over all classes; the
- * sequence is captured as a CUDA graph on the first call with a given set of pointers and
- * replayed on later calls with the same pointers.  Calls on one group must be serialised (they
- * share the group's intermediate buffers). */
+ * s2g_group_layout returns the offsets.  A call runs each phi-FFT and DCT stage as at most two
+ * grouped launches over all bandwidth classes (short transforms, bw <= 64, and long ones, run
+ * concurrently) and ONE persistent tensor-core contraction launch over all classes; the sequence
+ * is captured as a CUDA graph on the first call with a given set of pointers and replayed on later
+ * calls with the same pointers.  Calls on one group must be serialised (they share the group's
+ * intermediate buffers). */
 typedef struct s2g_group_s* s2g_group;
 int s2g_group_create(s2g_group* group, int nfunc, const int* bw, int precision);
 int s2g_group_destroy(s2g_group group);
@@ -307,14 +308,17 @@ int s2g_group_inv_fst(s2g_group group, const float* rcoeffs, const float* icoeff
 /* forward of grid into the coefficients, then inverse of those into grid_out, one graph */
 int s2g_group_fst_inv(s2g_group group, const float* grid, float* rcoeffs, float* icoeffs, float* grid_out,
                       void* stream);
-/* Times candidate tile shapes (N extent of each class's contraction tile, CTAs per SM of the
- * persistent kernel) on the group's sizes and keeps the fastest.  Results are cached per
+/* Times candidate shapes (N extent of each class's contraction tile, CTAs per SM of the
+ * persistent contraction, resident blocks per SM the DCT stages are sized for) on the group's
+ * whole forward + inverse sequence and keeps the fastest.  Results are cached per
  * (device, precision, class sizes); force != 0 re-measures.  $S2G_TUNE_CACHE, when set, names a
  * file that keeps them across processes.  Synchronous. */
 int s2g_group_autotune(s2g_group group, int force);
 /* Sets the shapes by hand: ctas_per_sm (0 = as many as fit) and one tile N per bandwidth class
  * in increasing bandwidth (0 = the class's whole table-row extent; NULL = all 0). */
 int s2g_group_set_tiles(s2g_group group, int ctas_per_sm, const int* tile_n);
+/* Sets the resident blocks per SM the grouped DCT stages are sized for (0 = as many as fit). */
+int s2g_group_set_dct_ctas(s2g_group group, int dct_ctas_per_sm);
 /* JSON description: classes [bw, count], chosen tiles, kernels per captured graph. */
 int s2g_group_describe(s2g_group group, char* buf, size_t len);
 /* Waits for the device and reports a failure recorded by the tensor-core kernels. */

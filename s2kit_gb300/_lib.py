@@ -85,6 +85,7 @@ SIGNATURES = {
     "s2g_group_fst_inv": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "s2g_group_autotune": (C.c_int, [vp, C.c_int]),
     "s2g_group_set_tiles": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
+    "s2g_group_set_dct_ctas": (C.c_int, [vp, C.c_int]),
     "s2g_group_describe": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
     "s2g_group_sync_status": (C.c_int, [vp]),
     "s2g_set_contraction_kernel": (C.c_int, [C.c_int]),

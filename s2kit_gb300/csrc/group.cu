@@ -3,19 +3,24 @@
 // A group fixes a list of functions (function f has bandwidth bw[f], a power of two in
 // [16, 512]) and a split precision.  Functions are binned by bandwidth into classes; each
 // class owns class-contiguous intermediate arrays.  One transform runs as
-//   forward : per class (on its own forked stream) the phi-DFT and the weighted DCT-II
-//             (FST_semi_memo.c:81-90, seminaive.c:161-176), then ONE persistent tcgen05
-//             contraction launch over the work items of every class (seminaive.c:183-197);
-//   inverse : ONE persistent contraction launch (seminaive.c:74-98), then per class the
-//             DCT-III, naive-order recombination and DFT over the orders (FST_semi_memo.c:334-350).
-// The sequence is captured once as a CUDA graph (on an internal stream, with the class
-// stages as parallel branches) and replayed on the caller's stream; the first call with a
-// given set of pointers runs eagerly and captures, later calls replay.
+//   forward : the phi-DFT of the classes (FST_semi_memo.c:81-90), then their weighted DCT-II
+//             (seminaive.c:161-176), then ONE persistent tcgen05 contraction launch over the work
+//             items of every class (seminaive.c:183-197);
+//   inverse : ONE persistent contraction launch (seminaive.c:74-98), then the DCT-III with the
+//             naive-order recombination, then the DFT over the orders (FST_semi_memo.c:334-350).
+// Each FFT stage is a grouped launch (k_stage_group: a block decodes its class and runs that
+// class's transform length) over a tier of classes: the short transforms (bw <= 64), compiled
+// for the per-length kernels' small register budgets, and the long ones (bw >= 128).  The two
+// tiers run concurrently on two streams, so a stage is at most two launches whatever the number
+// of classes.  The sequence is captured once as a CUDA graph (on an internal stream, the tiers as
+// parallel branches) and replayed on the caller's stream; the first call with a given set of
+// pointers runs eagerly and captures, later calls replay.
 //
-// Tile shapes (the N extent of each class's contraction tile, CTAs per SM of the persistent
-// kernel) come from an autotuner that times candidate shapes on the group's own sizes and
-// keeps the fastest; results are cached per (device, precision, class sizes) in memory and,
-// when $S2G_TUNE_CACHE names a file, on disk.
+// Shapes (the N extent of each class's contraction tile, CTAs per SM of the persistent
+// contraction, resident blocks per SM the DCT stages are sized for) come from an autotuner that
+// times the group's whole forward + inverse sequence on its own sizes and keeps the fastest;
+// results are cached per (device, precision, class sizes) in memory and, when $S2G_TUNE_CACHE
+// names a file, on disk.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -58,10 +63,11 @@ struct s2g_group_s {
     std::vector<s2g::GroupClass> cls;
     void* mem = nullptr;        // one device allocation: maps, intermediates, counters
     int* counters = nullptr;    // [0] forward, [1] inverse contraction work counters
-    int ctas_per_sm = 0;        // 0: as many as fit
+    int ctas_per_sm = 0;        // contraction: 0 = as many as fit
+    int dct_ctas = 0;           // DCT stages: resident blocks per SM they are sized for, 0 = as many as fit
     cudaStream_t cap = nullptr;
-    cudaStream_t side[s2g::kGroupMaxClasses] = {};
-    cudaEvent_t fork = nullptr, mid = nullptr, join[s2g::kGroupMaxClasses] = {};
+    cudaStream_t side = nullptr;               // the short-transform tier's stream
+    cudaEvent_t fork = nullptr, join = nullptr;
     s2g::GroupGraph graphs[3];  // forward, inverse, forward+inverse
     std::string tuning;         // description of the chosen tile shapes
 };
@@ -70,17 +76,46 @@ namespace s2g {
 
 // ---- launch sequences (eager or under capture) ----
 
-static int group_fwd_seq(s2g_group g, const float* grid, float* rc, float* ic, cudaStream_t st) {
-    S2G_CUDA(cudaEventRecord(g->fork, st));
+// Short transforms (bw <= 64) form one tier of the FFT stages, the rest the other.
+static constexpr int kShortTierMaxBw = 64;
+
+// FFT stage `which` of every class, from in(c) to out(c): the long tier on st, the short tier on the
+// side stream (forked from and joined back into st).
+template <typename In, typename Out>
+static int group_stages(s2g_group g, const int* which, int nstage, In in, Out out, cudaStream_t st) {
     const int nc = (int)g->cls.size();
-    for (int c = 0; c < nc; ++c) {
-        GroupClass& k = g->cls[c];
-        cudaStream_t s = g->side[c];
-        S2G_CUDA(cudaStreamWaitEvent(s, g->fork, 0));
-        S2G_TRY(split_fwd_head(k.t, grid, k.buf0, k.buf1, k.N, k.gmap, s));
-        S2G_CUDA(cudaEventRecord(g->join[c], s));
-        S2G_CUDA(cudaStreamWaitEvent(st, g->join[c], 0));
+    StageSpec lo[kGroupMaxClasses], hi[kGroupMaxClasses];
+    int nlo = 0, nhi = 0;
+    for (int w = 0; w < nstage; ++w) {
+        nlo = nhi = 0;
+        for (int c = 0; c < nc; ++c) {
+            GroupClass& k = g->cls[c];
+            const bool rows = which[w] == 0 || which[w] == 3;
+            const StageSpec q{k.t, k.N, in(w, c), out(w, c), rows ? k.gmap : nullptr};
+            if (k.B <= kShortTierMaxBw) lo[nlo++] = q;
+            else hi[nhi++] = q;
+        }
+        if (w == 0 && nlo && nhi) {
+            S2G_CUDA(cudaEventRecord(g->fork, st));
+            S2G_CUDA(cudaStreamWaitEvent(g->side, g->fork, 0));
+        }
+        const int dc = (which[w] == 1 || which[w] == 2) ? g->dct_ctas : 0;
+        if (nhi) S2G_TRY(split_stage_group(which[w], hi, nhi, dc, st));
+        if (nlo) S2G_TRY(split_stage_group(which[w], lo, nlo, dc, nhi ? g->side : st));
     }
+    if (nlo && nhi) {
+        S2G_CUDA(cudaEventRecord(g->join, g->side));
+        S2G_CUDA(cudaStreamWaitEvent(st, g->join, 0));
+    }
+    return S2G_OK;
+}
+
+static int group_fwd_seq(s2g_group g, const float* grid, float* rc, float* ic, cudaStream_t st) {
+    const int nc = (int)g->cls.size();
+    const int which[2] = {0, 1};  // grid -> X -> C
+    S2G_TRY(group_stages(
+        g, which, 2, [&](int w, int c) -> const void* { return w == 0 ? (const void*)grid : g->cls[c].buf0; },
+        [&](int w, int c) -> void* { return w == 0 ? g->cls[c].buf0 : g->cls[c].buf1; }, st));
     LegSpec spec[kGroupMaxClasses] = {};
     for (int c = 0; c < nc; ++c) {
         GroupClass& k = g->cls[c];
@@ -113,16 +148,10 @@ static int group_inv_seq(s2g_group g, const float* rc, const float* ic, float* g
         q.cmap = k.cmap;
     }
     S2G_TRY(split_leg(false, g->precision, spec, nc, g->counters + 1, g->ctas_per_sm, st));
-    S2G_CUDA(cudaEventRecord(g->mid, st));
-    for (int c = 0; c < nc; ++c) {
-        GroupClass& k = g->cls[c];
-        cudaStream_t s = g->side[c];
-        S2G_CUDA(cudaStreamWaitEvent(s, g->mid, 0));
-        S2G_TRY(split_inv_tail(k.t, k.buf0, k.buf1, grid, k.N, k.gmap, s));
-        S2G_CUDA(cudaEventRecord(g->join[c], s));
-        S2G_CUDA(cudaStreamWaitEvent(st, g->join[c], 0));
-    }
-    return S2G_OK;
+    const int which[2] = {2, 3};  // Fc -> F -> grid
+    return group_stages(
+        g, which, 2, [&](int w, int c) -> const void* { return w == 0 ? g->cls[c].buf1 : g->cls[c].buf0; },
+        [&](int w, int c) -> void* { return w == 0 ? (void*)g->cls[c].buf0 : (void*)grid; }, st);
 }
 
 static int group_seq(s2g_group g, int kind, const void* const* ptr, cudaStream_t st) {
@@ -182,7 +211,7 @@ static bool g_tune_loaded = false;
 static std::string tune_key(s2g_group g) {
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, g->device);
-    std::string k = std::string(prop.name) + "|p" + std::to_string(g->precision);
+    std::string k = std::string(prop.name) + "|v2|p" + std::to_string(g->precision);
     for (auto& c : g->cls) k += "|" + std::to_string(c.B) + "x" + std::to_string(c.N);
     for (auto& ch : k)
         if (ch == ' ') ch = '_';
@@ -219,7 +248,7 @@ static void tune_store(const std::string& key, const std::string& val) {
 }
 
 static std::string tune_value(s2g_group g) {
-    std::string v = std::to_string(g->ctas_per_sm);
+    std::string v = std::to_string(g->ctas_per_sm) + " " + std::to_string(g->dct_ctas);
     for (auto& c : g->cls) v += " " + std::to_string(c.NB);
     return v;
 }
@@ -234,14 +263,16 @@ static bool tune_apply(s2g_group g, const std::string& v) {
         x.push_back((int)a);
         p = end;
     }
-    if (x.size() != g->cls.size() + 1) return false;
+    if (x.size() != g->cls.size() + 2) return false;
     g->ctas_per_sm = x[0];
-    for (size_t c = 0; c < g->cls.size(); ++c) g->cls[c].NB = x[c + 1];
+    g->dct_ctas = x[1];
+    for (size_t c = 0; c < g->cls.size(); ++c) g->cls[c].NB = x[c + 2];
     return true;
 }
 
 static void tune_describe(s2g_group g) {
-    std::string d = "{\"ctas_per_sm\": " + std::to_string(g->ctas_per_sm) + ", \"tile_n\": {";
+    std::string d = "{\"ctas_per_sm\": " + std::to_string(g->ctas_per_sm) +
+                    ", \"dct_ctas_per_sm\": " + std::to_string(g->dct_ctas) + ", \"tile_n\": {";
     for (size_t c = 0; c < g->cls.size(); ++c) {
         if (c) d += ", ";
         d += "\"" + std::to_string(g->cls[c].B) + "\": " + std::to_string(g->cls[c].NB);
@@ -258,24 +289,18 @@ static std::vector<int> nb_candidates(int B) {
     return v;
 }
 
-// Times forward + inverse contraction launches with the current shapes (ms, best of reps).
-static int time_contractions(s2g_group g, const float* grid, float* rc, float* ic, int reps, float* ms) {
+// Times the group's forward + inverse sequence with the current shapes on the internal stream
+// (ms, best of reps; eager launches, so shape changes need no new graph).
+static int time_group(s2g_group g, const float* grid, float* rc, float* ic, float* grid_out, int reps, float* ms) {
     cudaEvent_t a, b;
     S2G_CUDA(cudaEventCreate(&a));
     S2G_CUDA(cudaEventCreate(&b));
     float best = 1e30f;
     int r = S2G_OK;
-    const int nc = (int)g->cls.size();
     for (int it = 0; it < reps + 1 && r == S2G_OK; ++it) {
-        LegSpec f[kGroupMaxClasses] = {}, iv[kGroupMaxClasses] = {};
-        for (int c = 0; c < nc; ++c) {
-            GroupClass& k = g->cls[c];
-            f[c] = LegSpec{k.t, k.N, k.NB, k.buf1, k.buf0, nullptr, nullptr, rc, ic, nullptr, nullptr, k.cmap};
-            iv[c] = LegSpec{k.t, k.N, k.NB, nullptr, nullptr, rc, ic, nullptr, nullptr, k.buf1, k.buf0, k.cmap};
-        }
         cudaEventRecord(a, g->cap);
-        r = split_leg(true, g->precision, f, nc, g->counters, g->ctas_per_sm, g->cap);
-        if (r == S2G_OK) r = split_leg(false, g->precision, iv, nc, g->counters + 1, g->ctas_per_sm, g->cap);
+        r = group_fwd_seq(g, grid, rc, ic, g->cap);
+        if (r == S2G_OK) r = group_inv_seq(g, rc, ic, grid_out, g->cap);
         cudaEventRecord(b, g->cap);
         if (cudaEventSynchronize(b) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "autotune");
         float t = 0;
@@ -284,7 +309,6 @@ static int time_contractions(s2g_group g, const float* grid, float* rc, float* i
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    (void)grid;
     *ms = best;
     return r;
 }
@@ -300,20 +324,21 @@ static int group_autotune(s2g_group g, int force) {
             return S2G_OK;
         }
     }
-    // synthetic coefficients and intermediates: the contraction's cost does not depend on values
+    // synthetic samples and coefficients (zero): the kernels' cost does not depend on values
     float* rc = nullptr;
-    S2G_CUDA(cudaMalloc(&rc, 2 * sizeof(float) * (size_t)g->coef_total));
+    const size_t nbuf = 2 * (size_t)g->coef_total + 2 * (size_t)g->grid_total;
+    S2G_CUDA(cudaMalloc(&rc, sizeof(float) * nbuf));
     float* ic = rc + g->coef_total;
-    S2G_CUDA(cudaMemsetAsync(rc, 0, 2 * sizeof(float) * (size_t)g->coef_total, g->cap));
-    for (auto& c : g->cls) {
-        S2G_CUDA(cudaMemsetAsync(c.buf0, 0, sizeof(float) * 2 * (size_t)c.N * c.B * 2 * c.B, g->cap));
-        S2G_CUDA(cudaMemsetAsync(c.buf1, 0, sizeof(float) * 2 * (size_t)c.N * c.B * c.B, g->cap));
-    }
+    float* grid = ic + g->coef_total;
+    float* grid_out = grid + g->grid_total;
+    S2G_CUDA(cudaMemsetAsync(rc, 0, sizeof(float) * nbuf, g->cap));
     int r = S2G_OK;
     float best = 0;
     g->ctas_per_sm = 0;
+    g->dct_ctas = 0;
     for (auto& c : g->cls) c.NB = 0;
-    r = time_contractions(g, nullptr, rc, ic, 3, &best);
+    auto timed = [&](float* ms) { return time_group(g, grid, rc, ic, grid_out, 3, ms); };
+    r = timed(&best);
     // coordinate descent: classes with the most work first, then the persistent grid size
     std::vector<int> order(g->cls.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
@@ -330,7 +355,7 @@ static int group_autotune(s2g_group g, int force) {
             if (nb == keep) continue;
             c.NB = nb;
             float ms = 0;
-            r = time_contractions(g, nullptr, rc, ic, 3, &ms);
+            r = timed(&ms);
             if (r != S2G_OK) break;
             if (ms < best * 0.98f) best = ms, keep = nb;
         }
@@ -341,9 +366,18 @@ static int group_autotune(s2g_group g, int force) {
         const int keep = g->ctas_per_sm;
         g->ctas_per_sm = cps;
         float ms = 0;
-        r = time_contractions(g, nullptr, rc, ic, 3, &ms);
+        r = timed(&ms);
         if (r == S2G_OK && ms < best * 0.98f) best = ms;
         else g->ctas_per_sm = keep;
+    }
+    for (int dc : {1, 2, 3, 4}) {
+        if (r != S2G_OK) break;
+        const int keep = g->dct_ctas;
+        g->dct_ctas = dc;
+        float ms = 0;
+        r = timed(&ms);
+        if (r == S2G_OK && ms < best * 0.98f) best = ms;
+        else g->dct_ctas = keep;
     }
     cudaStreamSynchronize(g->cap);
     cudaFree(rc);
@@ -359,13 +393,11 @@ static void group_free(s2g_group g) {
     if (g->device >= 0) cudaSetDevice(g->device);
     if (g->cap) cudaStreamSynchronize(g->cap);
     for (auto& gr : g->graphs) drop_graph(gr);
-    for (auto s : g->side)
-        if (s) cudaStreamDestroy(s);
+    if (g->side) cudaStreamSynchronize(g->side);
+    if (g->side) cudaStreamDestroy(g->side);
     if (g->cap) cudaStreamDestroy(g->cap);
-    for (auto e : g->join)
-        if (e) cudaEventDestroy(e);
     if (g->fork) cudaEventDestroy(g->fork);
-    if (g->mid) cudaEventDestroy(g->mid);
+    if (g->join) cudaEventDestroy(g->join);
     cudaFree(g->mem);
     for (auto& c : g->cls) put_tables(c.t);
     delete g;
@@ -455,12 +487,9 @@ int s2g_group_create(s2g_group* out, int nfunc, const int* bw, int precision) {
     };
     if (r == S2G_OK) {
         ck(cudaStreamCreateWithFlags(&g->cap, cudaStreamNonBlocking), "cudaStreamCreate");
-        for (size_t c = 0; c < g->cls.size(); ++c)
-            ck(cudaStreamCreateWithFlags(&g->side[c], cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking), "cudaStreamCreate");
         ck(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming), "cudaEventCreate");
-        ck(cudaEventCreateWithFlags(&g->mid, cudaEventDisableTiming), "cudaEventCreate");
-        for (size_t c = 0; c < g->cls.size(); ++c)
-            ck(cudaEventCreateWithFlags(&g->join[c], cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&g->join, cudaEventDisableTiming), "cudaEventCreate");
     }
     // operands packed now, so that no later call allocates (a graph capture cannot)
     for (auto& c : g->cls)
@@ -535,6 +564,16 @@ int s2g_group_set_tiles(s2g_group g, int ctas_per_sm, const int* tile_n) {
             return fail(S2G_ERR_ARG, "tile_n[%zu] = %d: a multiple of 16 in [0, 256]", c, tile_n[c]);
     g->ctas_per_sm = ctas_per_sm;
     for (size_t c = 0; c < g->cls.size(); ++c) g->cls[c].NB = tile_n ? tile_n[c] : 0;
+    for (auto& gr : g->graphs) drop_graph(gr);
+    tune_describe(g);
+    return S2G_OK;
+}
+
+int s2g_group_set_dct_ctas(s2g_group g, int dct_ctas_per_sm) {
+    S2G_TRY(group_check(g));
+    if (dct_ctas_per_sm < 0 || dct_ctas_per_sm > 8)
+        return fail(S2G_ERR_ARG, "dct_ctas_per_sm %d outside [0, 8]", dct_ctas_per_sm);
+    g->dct_ctas = dct_ctas_per_sm;
     for (auto& gr : g->graphs) drop_graph(gr);
     tune_describe(g);
     return S2G_OK;

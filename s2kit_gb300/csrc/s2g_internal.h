@@ -153,6 +153,19 @@ int fst_split_complex(Tables* t, const float* rgrid, const float* igrid, float* 
                       int precision, void* work, void* cwork, cudaStream_t st);
 int inv_fst_split_complex(Tables* t, const float* rc, const float* ic, float* rgrid, float* igrid, int batch,
                           int precision, void* work, void* cwork, cudaStream_t st);
+// One FFT stage of several bandwidth classes (split path, power-of-two bw <= 512) in ONE launch:
+// which 0 rows forward (grid -> X), 1 weighted DCT-II (X -> C), 2 DCT-III (Fc -> F), 3 rows
+// inverse (F -> grid); in/out as the per-class kernels, gmap per-function grid offsets for the
+// rows stages.  dct_ctas_per_sm bounds the resident blocks the DCT stages are sized for (0: as
+// many as fit).
+struct StageSpec {
+    Tables* t;
+    int N;
+    const void* in;
+    void* out;
+    const int64_t* gmap;
+};
+int split_stage_group(int which, const StageSpec* spec, int ncls, int dct_ctas_per_sm, cudaStream_t st);
 // Reads (and optionally clears) the device error word of the tensor-core kernels.
 int split_device_status(Tables* t, int clear);
 

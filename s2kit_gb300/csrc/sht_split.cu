@@ -18,6 +18,7 @@
 // Precision: x = x0 + x1 + x2 with BF16 terms (each the rounded residual of the previous);
 // the table is split the same way from FP64.  S2G_PREC_BF16X3 sums the six products
 // x_a t_b with a + b <= 2, S2G_PREC_BF16X2 the three with a + b <= 1.
+#include <limits.h>
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -461,10 +462,25 @@ struct FftSmem {
 // Each warp leaves its spectrum in shared memory; the separation of the two packed real rows,
 // X_a = (Z[m] + conj Z[S-m]) / 2 and X_b = (Z[m] - conj Z[S-m]) / 2i, is done by the threads
 // that write the transposed tile, each a float4 run of 4 latitudes of one order.
-template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasFwd)
-    k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N, float scale,
-                 const float2* __restrict__ gtw, const int64_t* __restrict__ gmap) {
+// The FFT kernels' bodies: with G the block index vb and block count vgrid come as arguments, so
+// that the grouped stage kernels (k_stage_group) run the same code over several bandwidth classes;
+// without G they are blockIdx.x and gridDim.x, used where and as (unsigned) the per-length
+// kernels always used them, which keeps those kernels' register allocation.
+template <bool G>
+__device__ __forceinline__ auto vblock(int vb) {
+    if constexpr (G) return vb;
+    else return blockIdx.x;
+}
+template <bool G>
+__device__ __forceinline__ auto vgridn(int vgrid) {
+    if constexpr (G) return vgrid;
+    else return gridDim.x;
+}
+
+template <int R, bool G>
+__device__ __forceinline__ void rows_fwd_body(const float* __restrict__ grid, float* __restrict__ X, int N,
+                                              float scale, const float2* __restrict__ gtw,
+                                              const int64_t* __restrict__ gmap, int vb, int vgrid) {
     using L = FftSmem<R>;
     constexpr int S = L::S, B = L::B, PSA = L::PSA;
     constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
@@ -483,7 +499,7 @@ __global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasFwd)
     __syncthreads();
     // CTA-strided (function, latitude block) tiles; launched with one tile per CTA
     constexpr int NLB = S / LAT;
-    for (int tile = blockIdx.x; tile < N * NLB; tile += gridDim.x) {
+    for (int tile = vblock<G>(vb); tile < N * NLB; tile += vgridn<G>(vgrid)) {
     const int f = tile / NLB, th0 = (tile - f * NLB) * LAT;
     const float* ra = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + 2 * warp) * S;
     float* wr = spr + warp * PSA;
@@ -546,16 +562,23 @@ __global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasFwd)
     }
 }
 
+template <int R>
+__global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasFwd)
+    k_rows_fwd_w(const float* __restrict__ grid, float* __restrict__ X, int N, float scale,
+                 const float2* __restrict__ gtw, const int64_t* __restrict__ gmap) {
+    rows_fwd_body<R, false>(grid, X, N, scale, gtw, gmap, 0, 0);
+}
+
 // Weighted REDFT10 per (function, seminaive order) row, stored by parity of the cosine index:
 // C[p][f][m][t][j] holds frequency k = 2j + t (j < B/2), so that the contraction's operand rows
 // of one parity are contiguous.  Naive orders are folded in place in X for their contraction:
 // X[p][f][m][t][j] = x[j] + (-1)^t x[S-1-j], j < B (the even/odd latitude halves).
 // Seminaive rows are read straight into the FFT's registers (4- or 8-byte loads) and leave in
 // 16-byte pieces through the warp's spectrum buffer; naive rows go through it both ways.
-template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict__ X, float* __restrict__ Cout, int nrows,
-                                                   const float* __restrict__ gw, const float2* __restrict__ gtw,
-                                                   const float2* __restrict__ gtwD) {
+template <int R, bool G>
+__device__ __forceinline__ void dct_fwd_body(float* __restrict__ X, float* __restrict__ Cout, int nrows,
+                                             const float* __restrict__ gw, const float2* __restrict__ gtw,
+                                             const float2* __restrict__ gtwD, int vb, int vgrid) {
     using L = FftSmem<R>;
     constexpr int S = L::S, B = L::B, PSA = L::PSA;
     constexpr int W = FftShape<R>::W;
@@ -579,7 +602,7 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // persistent: the tables are loaded once, then each warp walks rows
-    for (int row = blockIdx.x * W + warp; row < nrows; row += gridDim.x * W) {
+    for (int row = vblock<G>(vb) * W + warp; row < nrows; row += vgridn<G>(vgrid) * W) {
     const int m = row % B;
     float* xr = X + (size_t)row * S;
     float* xi = xr + (size_t)nrows * S;
@@ -673,13 +696,20 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict_
     }
 }
 
+template <int R>
+__global__ void __launch_bounds__(FftShape<R>::T) k_dct_fwd_w(float* __restrict__ X, float* __restrict__ Cout, int nrows,
+                                                   const float* __restrict__ gw, const float2* __restrict__ gtw,
+                                                   const float2* __restrict__ gtwD) {
+    dct_fwd_body<R, false>(X, Cout, nrows, gw, gtw, gtwD, 0, 0);
+}
+
 // REDFT01 per (function, seminaive order) row, sin(theta) for odd m, scale: F[p][f][m][theta].
 // Seminaive rows arrive through the warp's cp.async prefetch buffer (R <= 16) or straight from
 // global memory, and leave in 16-byte pieces through the warp's spectrum buffer.
-template <int R>
-__global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
-                                                   const float* __restrict__ gsin, const float2* __restrict__ gtw,
-                                                   const float2* __restrict__ gtwD, float scale) {
+template <int R, bool G>
+__device__ __forceinline__ void dct_inv_body(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
+                                             const float* __restrict__ gsin, const float2* __restrict__ gtw,
+                                             const float2* __restrict__ gtwD, float scale, int vb, int vgrid) {
     using L = FftSmem<R>;
     constexpr int S = L::S, B = L::B, PSA = L::PSA;
     constexpr int W = FftShape<R>::W;
@@ -710,7 +740,7 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
     float* zr = spr + warp * PSA;
     float* zi = spi + warp * PSA;
     float* pf = pfb + warp * 2 * PB;
-    const int rstride = gridDim.x * W;
+    const int rstride = vgridn<G>(vgrid) * W;
     // asynchronous copy of row r's two planes (B/4 16-byte pieces each) into the warp's buffer;
     // naive-order rows and rows past the end copy nothing.  One commit group per call.
     auto prefetch = [&](int r) {
@@ -722,9 +752,9 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
         }
         tc::cp_async_commit();
     };
-    if constexpr (kPf) prefetch(blockIdx.x * W + warp);
+    if constexpr (kPf) prefetch(vblock<G>(vb) * W + warp);
     // persistent: the tables are loaded once, then each warp walks rows
-    for (int row = blockIdx.x * W + warp; row < nrows; row += rstride) {
+    for (int row = vblock<G>(vb) * W + warp; row < nrows; row += rstride) {
     const int m = row % B;
     if (naive_order(m)) {
         // the buffer is idle during a naive row: the next row's copy starts now
@@ -818,155 +848,113 @@ __global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __res
 // DFT with sign +1 over the orders for LAT latitudes (two real output rows per warp).  The
 // order-major input arrives as float4 runs of 4 latitudes; output rows leave as 128-byte lines
 // from registers (R = 8, 16, 32) or as float4 through the warp's spectrum buffer.
+template <int R, bool G>
+__device__ __forceinline__ void rows_inv_body(const float* __restrict__ F, float* __restrict__ grid, int N,
+                                              const float2* __restrict__ gtw, const int64_t* __restrict__ gmap,
+                                              int vb, int vgrid) {
+#include "rows_inv_body.inc"
+}
+
 template <int R>
 __global__ void __launch_bounds__(FftShape<R>::T, FftShape<R>::kMinCtasInv)
     k_rows_inv_w(const float* __restrict__ F, float* __restrict__ grid, int N, const float2* __restrict__ gtw,
                  const int64_t* __restrict__ gmap) {
+    constexpr bool G = false;
+    constexpr int vb = 0, vgrid = 0;
+#include "rows_inv_body.inc"
+}
+
+template <int R>
+__global__ void __launch_bounds__(FftShape<R>::T) k_dct_inv_w(const float* __restrict__ Fc, float* __restrict__ F, int nrows,
+                                                   const float* __restrict__ gsin, const float2* __restrict__ gtw,
+                                                   const float2* __restrict__ gtwD, float scale) {
+    dct_inv_body<R, false>(Fc, F, nrows, gsin, gtw, gtwD, scale, 0, 0);
+}
+
+// Dynamic shared memory of FFT kernel `which` (0 rows forward, 1 DCT-II, 2 DCT-III, 3 rows inverse)
+// at length S = 32 R.
+template <int R>
+static size_t fft_smem(int which) {
+    constexpr int S = 32 * R, B = S / 2;
+    constexpr int kWarps = FftShape<R>::W, kLatPerCta = FftShape<R>::LAT;
     using L = FftSmem<R>;
-    constexpr int S = L::S, B = L::B, PSA = L::PSA, TS = L::TS;
-    constexpr int W = FftShape<R>::W, LAT = FftShape<R>::LAT, T = FftShape<R>::T;
-    static_assert(S % LAT == 0 && LAT % 4 == 0, "row staging");
-    extern __shared__ __align__(16) float fsm[];
-    // R = 8, 16: the tile (re, im) holds latitude pairs: latitude th0 + lat of order m at
-    // [(lat / 2) * PS + 2 m + (lat & 1)], PS = 2 TS = 2B + 4 floats (4 mod 32), so that a float4 of 4
-    // latitudes goes in as two conflict-free 8-byte stores and a warp reads its pair (a, b) of one
-    // order with one 8-byte load per plane (-2% at R = 16; +2-3% at R = 4 and 32, which keep the
-    // latitude-major [LAT][TS]).  Either tile is dead once every warp holds its inputs; the warps'
-    // spectrum buffers [W][PSA] (re, im) then reuse the same space.
-    constexpr bool kPairTile = R == 8 || R == 16;
-    constexpr int PS = 2 * TS;
-    constexpr int U = 2 * LAT * TS > 2 * W * PSA ? 2 * LAT * TS : 2 * W * PSA;
-    float* tr = fsm;
-    float* ti = tr + (LAT / 2) * PS;
-    float* spr = fsm;
-    float* spi = spr + W * PSA;
-    float2* tw = reinterpret_cast<float2*>(fsm + U);
-    float2* twb = tw + (R == 64 ? twtab_len(S / 2) : twtab_len(S));
-    float2* twc = twb + S / 2;  // R = 64 only
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if constexpr (R == 64)
-        load_tw_split(tw, twb, twc, gtw);
+    const size_t tw_bytes = sizeof(float2) * (twtab_len(S) + S), spec = sizeof(float) * 2 * kWarps * L::PSA;
+    switch (which) {
+        case 0: return spec + tw_bytes;
+        case 1: return spec + sizeof(float) * 2 * S + sizeof(float2) * B + tw_bytes;
+        case 2:
+            return spec + (L::kDctInvPf ? sizeof(float) * kWarps * 2 * L::PB : 0) + sizeof(float) * S +
+                   sizeof(float2) * S + tw_bytes;
+        default: return std::max(sizeof(float) * 2 * kLatPerCta * L::TS, spec) + tw_bytes;
+    }
+}
+
+// ---- grouped stage kernels: one launch runs one FFT stage of several bandwidth classes ----
+// Blocks [blk0, blk0 + nblk) belong to class c; each class runs the body of its own length with
+// block index blockIdx.x - blk0 among nblk.  The row kernels take one (function, latitude block)
+// tile per block; the DCT kernels stride their blocks over the class's rows, so a class's block
+// count sets how many rows share one load of its twiddle tables.
+static constexpr int kStageMaxClasses = 6;
+
+struct StageCls {
+    int R, blk0, nblk, N;
+    const void* in;
+    void* out;
+    const int64_t* gmap;   // rows kernels: per-function grid offsets (null: f * S * S)
+    const float* w32;      // DCT-II: weights
+    const float* sin32;    // DCT-III: sin(theta)
+    const float2* twS;
+    const float2* twD;
+    float scale;
+};
+
+struct StageArgs {
+    int ncls;
+    StageCls c[kStageMaxClasses];
+};
+
+template <int WHICH, int R>
+__device__ __forceinline__ void stage_body(const StageCls& k, int vb) {
+    const int B = 16 * R;
+    if constexpr (WHICH == 0)
+        rows_fwd_body<R, true>((const float*)k.in, (float*)k.out, k.N, k.scale, k.twS, k.gmap, vb, k.nblk);
+    else if constexpr (WHICH == 1)
+        dct_fwd_body<R, true>((float*)k.in, (float*)k.out, k.N * B, k.w32, k.twS, k.twD, vb, k.nblk);
+    else if constexpr (WHICH == 2)
+        dct_inv_body<R, true>((const float*)k.in, (float*)k.out, k.N * B, k.sin32, k.twS, k.twD, k.scale, vb, k.nblk);
     else
-        load_tw(tw, twb, nullptr, gtw, nullptr, S);
-    const size_t plane = (size_t)N * B * S;
-    // CTA-strided (function, latitude block) tiles; launched with one tile per CTA
-    constexpr int NLB = S / LAT;
-    for (int tile = blockIdx.x; tile < N * NLB; tile += gridDim.x) {
-    const int f = tile / NLB, th0 = (tile - f * NLB) * LAT;
-    constexpr int Q4 = LAT / 4;
-    // loads of up to four iterations are issued before their shared-memory stores
-    constexpr int NIT = (B * Q4 + T - 1) / T, BAT = NIT < 4 ? NIT : 4;
-    for (int it0 = 0; it0 < NIT; it0 += BAT) {
-        float4 a[BAT], b[BAT];
-#pragma unroll
-        for (int u = 0; u < BAT; ++u) {
-            const int e = threadIdx.x + (it0 + u) * T;
-            if (e < B * Q4) {
-                const int m = e / Q4, q = 4 * (e - m * Q4);
-                const size_t o = ((size_t)f * B + m) * S + th0 + q;
-                a[u] = *reinterpret_cast<const float4*>(F + o);
-                b[u] = *reinterpret_cast<const float4*>(F + plane + o);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < BAT; ++u) {
-            const int e = threadIdx.x + (it0 + u) * T;
-            if (e < B * Q4) {
-                const int m = e / Q4, q = 4 * (e - m * Q4);
-                if constexpr (kPairTile) {
-                    float* pr = tr + (q / 2) * PS + 2 * m;
-                    float* pi = ti + (q / 2) * PS + 2 * m;
-                    *reinterpret_cast<float2*>(pr) = make_float2(a[u].x, a[u].y);
-                    *reinterpret_cast<float2*>(pr + PS) = make_float2(a[u].z, a[u].w);
-                    *reinterpret_cast<float2*>(pi) = make_float2(b[u].x, b[u].y);
-                    *reinterpret_cast<float2*>(pi + PS) = make_float2(b[u].z, b[u].w);
-                } else {
-                    float* pr = tr + q * TS + m;
-                    float* pi = ti + q * TS + m;
-                    pr[0] = a[u].x, pr[TS] = a[u].y, pr[2 * TS] = a[u].z, pr[3 * TS] = a[u].w;
-                    pi[0] = b[u].x, pi[TS] = b[u].y, pi[2 * TS] = b[u].z, pi[3 * TS] = b[u].w;
-                }
-            }
-        }
-    }
-    __syncthreads();
-    const int a = 2 * warp, b = a + 1;  // this warp's latitudes (pair row `warp` of a pair tile)
-    // latitudes a and b of order mm < B: (re_a, re_b) and (im_a, im_b)
-    auto at = [&](int mm, float2& re, float2& im) {
-        if constexpr (kPairTile) {
-            re = *reinterpret_cast<const float2*>(tr + warp * PS + 2 * mm);
-            im = *reinterpret_cast<const float2*>(ti + warp * PS + 2 * mm);
-        } else {
-            re = make_float2(tr[a * TS + mm], tr[b * TS + mm]);
-            im = make_float2(ti[a * TS + mm], ti[b * TS + mm]);
-        }
-    };
-    auto in = [&](int m) {
-        float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
-        float2 re, im;
-        if (m < B) {
-            at(m, re, im);
-            ar = re.x, br = re.y;
-            ai = (m == 0) ? 0.f : im.x;
-            bi = (m == 0) ? 0.f : im.y;
-        } else if (m > B) {
-            at(S - m, re, im);
-            ar = re.x, br = re.y;
-            ai = -im.x, bi = -im.y;
-        }
-        return make_float2(ar - bi, ai + br);  // F_a + i F_b
-    };
-    float* zr = spr + warp * PSA;
-    float* zi = spi + warp * PSA;
-    // the four-step form (R = 8, 16, 32) leaves 32 consecutive outputs in register k1 of the 32
-    // lanes: each store is one full 128-byte line of row a (real parts) or row b (imaginary
-    // parts), straight from registers.  The other forms stage the spectrum for float4 stores.
-    constexpr bool kDirect = R >= 8 && R <= 32;
-    if constexpr (R == 64) {
-        // both halves' inputs are gathered before the tile dies (its space becomes the spectra)
-        float2 ve[32], vo[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-            ve[i] = in(2 * (lane + 32 * i));
-            vo[i] = in(2 * (lane + 32 * i) + 1);
-        }
-        __syncthreads();  // the tile is dead: spectrum buffers below overwrite it
-        WarpFFT2048::to_spectrum_regs(ve, vo, tw, twb, twc, zr, zi, 1.f);
-    } else {
-        float2 v[R];
-#pragma unroll
-        for (int i = 0; i < R; ++i) v[i] = in(lane + 32 * i);
-        __syncthreads();  // the tile is dead: the exchange planes and spectra below overwrite it
-        WarpFFTSel<R>::run(v, tw, twb, zr, zi, 1.f);
-        if constexpr (kDirect) {
-            float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;
-#pragma unroll
-            for (int k1 = 0; k1 < R; ++k1) {
-                const int o = WarpFFTSel<R>::out_index(k1);
-                ga[o] = v[k1].x;
-                ga[S + o] = v[k1].y;
-            }
-        } else {
-#pragma unroll
-            for (int k1 = 0; k1 < R; ++k1) {
-                const int o = pad32(WarpFFTSel<R>::out_index(k1));
-                zr[o] = v[k1].x;
-                zi[o] = v[k1].y;
-            }
-        }
-    }
-    if constexpr (!kDirect) {
-        __syncwarp();
-        float* ga = grid + (gmap ? gmap[f] : (int64_t)f * S * S) + (size_t)(th0 + a) * S;
-        for (int e = lane; e < S / 4; e += 32) {
-            const int k = 4 * e;
-            reinterpret_cast<float4*>(ga)[e] =
-                make_float4(zr[pad32(k)], zr[pad32(k + 1)], zr[pad32(k + 2)], zr[pad32(k + 3)]);
-            reinterpret_cast<float4*>(ga + S)[e] =
-                make_float4(zi[pad32(k)], zi[pad32(k + 1)], zi[pad32(k + 2)], zi[pad32(k + 3)]);
-        }
-    }
-    __syncthreads();  // the exchange planes and spectra (aliasing the tile) are done before the next tile is loaded
+        rows_inv_body<R, true>((const float*)k.in, (float*)k.out, k.N, k.twS, k.gmap, vb, k.nblk);
+}
+
+// Resident CTAs per SM a grouped stage kernel is compiled for.  RMAX is the longest transform
+// (32 RMAX points) it carries, and only lengths up to RMAX are compiled in, so the short tier
+// (RMAX 4: bw <= 64) keeps the per-length kernels' small register budgets; the long tiers take
+// three CTAs (RMAX 16, bw <= 256; at four the row stages spill, the dispatch over lengths costing
+// registers the per-length kernels do not spend) and two (RMAX 32, bw 512).
+template <int WHICH, int RMAX>
+struct StageOcc {
+    static constexpr int v = RMAX <= 4 ? ((WHICH == 1 || WHICH == 2) ? 5 : 8) : RMAX <= 16 ? 3 : 2;
+};
+
+template <int WHICH, int RMAX>
+__global__ void __launch_bounds__(256, StageOcc<WHICH, RMAX>::v) k_stage_group(const __grid_constant__ StageArgs a) {
+    int ci = 0;
+    while (ci + 1 < a.ncls && (int)blockIdx.x >= a.c[ci + 1].blk0) ++ci;
+    const StageCls& k = a.c[ci];
+    const int vb = (int)blockIdx.x - k.blk0;
+    switch (k.R) {
+        case 1: stage_body<WHICH, 1>(k, vb); break;
+        case 2: stage_body<WHICH, 2>(k, vb); break;
+        case 4: stage_body<WHICH, 4>(k, vb); break;
+        case 8:
+            if constexpr (RMAX >= 8) stage_body<WHICH, 8>(k, vb);
+            break;
+        case 16:
+            if constexpr (RMAX >= 16) stage_body<WHICH, 16>(k, vb);
+            break;
+        default:
+            if constexpr (RMAX >= 32) stage_body<WHICH, 32>(k, vb);
+            break;
     }
 }
 
@@ -2462,17 +2450,13 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
     constexpr int S = 32 * R, B = S / 2;
     constexpr int kWarps = FftShape<R>::W, kLatPerCta = FftShape<R>::LAT, kThreads = FftShape<R>::T;
     const int nrows = N * B;
-    size_t smem = 0;
-    using L = FftSmem<R>;
-    const size_t tw_bytes = sizeof(float2) * (twtab_len(S) + S), spec = sizeof(float) * 2 * kWarps * L::PSA;
+    const size_t smem = fft_smem<R>(which);
     if (which == 0) {  // rows forward
-        smem = spec + tw_bytes;
         S2G_TRY(set_smem((const void*)k_rows_fwd_w<R>, smem));
         const int g = N * (S / kLatPerCta);  // one tile per CTA: fresh CTAs overlap loads better than a loop
         ProfScope ps_("rows_fwd_f32", st);
         k_rows_fwd_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, N, scale, s->twS, gmap);
     } else if (which == 1) {  // DCT-II
-        smem = spec + sizeof(float) * 2 * S + sizeof(float2) * B + tw_bytes;
         S2G_TRY(set_smem((const void*)k_dct_fwd_w<R>, smem));
         int g;
         S2G_TRY(persistent_grid((const void*)k_dct_fwd_w<R>, kThreads, smem, (nrows + kWarps - 1) / kWarps, &g));
@@ -2480,8 +2464,6 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
         k_dct_fwd_w<R><<<g, kThreads, smem, st>>>((float*)in, (float*)out, nrows, s->w32,
                                                                         s->twS, s->twD);
     } else if (which == 2) {  // DCT-III
-        smem = spec + (L::kDctInvPf ? sizeof(float) * kWarps * 2 * L::PB : 0) + sizeof(float) * S +
-               sizeof(float2) * S + tw_bytes;
         S2G_TRY(set_smem((const void*)k_dct_inv_w<R>, smem));
         int g;
         S2G_TRY(persistent_grid((const void*)k_dct_inv_w<R>, kThreads, smem, (nrows + kWarps - 1) / kWarps, &g));
@@ -2489,7 +2471,6 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
         k_dct_inv_w<R><<<g, kThreads, smem, st>>>((const float*)in, (float*)out, nrows,
                                                                         s->sin32, s->twS, s->twD, scale);
     } else {  // rows inverse
-        smem = std::max(sizeof(float) * 2 * kLatPerCta * L::TS, spec) + tw_bytes;
         S2G_TRY(set_smem((const void*)k_rows_inv_w<R>, smem));
         const int g = N * (S / kLatPerCta);  // one tile per CTA: fresh CTAs overlap loads better than a loop
         ProfScope ps_("rows_inv_f32", st);
@@ -2511,6 +2492,99 @@ static int fft_kernels(int which, int B, const void* in, void* out, int N, const
         case 64: return launch_fft_kernels<64>(which, in, out, N, s, st, scale, gmap);
         default: return fail(S2G_ERR_UNSUPPORTED, "no warp FFT for bandwidth %d", B);
     }
+}
+
+static size_t fft_smem_rt(int R, int which) {
+    switch (R) {
+        case 1: return fft_smem<1>(which);
+        case 2: return fft_smem<2>(which);
+        case 4: return fft_smem<4>(which);
+        case 8: return fft_smem<8>(which);
+        case 16: return fft_smem<16>(which);
+        case 32: return fft_smem<32>(which);
+        default: return fft_smem<64>(which);
+    }
+}
+
+template <int WHICH>
+static const void* stage_kernel(int rmax) {
+    return rmax <= 4 ? (const void*)k_stage_group<WHICH, 4>
+         : rmax <= 16 ? (const void*)k_stage_group<WHICH, 16> : (const void*)k_stage_group<WHICH, 32>;
+}
+
+int split_stage_group(int which, const StageSpec* spec, int ncls, int dct_ctas_per_sm, cudaStream_t st) {
+    if (ncls < 1 || ncls > kStageMaxClasses) return fail(S2G_ERR_ARG, "%d classes in one stage launch", ncls);
+    if (which < 0 || which > 3) return fail(S2G_ERR_ARG, "stage %d", which);
+    StageArgs a{};
+    a.ncls = ncls;
+    int rmax = 1;
+    size_t smem = 0;
+    double wsum = 0.0;
+    for (int c = 0; c < ncls; ++c) {
+        const StageSpec& q = spec[c];
+        S2G_TRY(build_split(q.t));
+        const Split* sp = (const Split*)q.t->split;
+        const int B = q.t->bw, S = 2 * B, R = S / 32;
+        if (R > 32) return fail(S2G_ERR_UNSUPPORTED, "grouped stages take bw <= 512 (got %d)", B);
+        StageCls& k = a.c[c];
+        k.R = R;
+        k.N = q.N;
+        k.in = q.in;
+        k.out = q.out;
+        k.gmap = q.gmap;
+        k.w32 = sp->w32;
+        k.sin32 = sp->sin32;
+        k.twS = sp->twS;
+        k.twD = sp->twD;
+        k.scale = which == 0 ? (float)(sqrt(2.0 * kPi) / S) : which == 2 ? (float)(1.0 / sqrt(2.0 * kPi)) : 1.f;
+        rmax = std::max(rmax, R);
+        smem = std::max(smem, fft_smem_rt(R, which));
+        wsum += (double)q.N * B * R;
+    }
+    const void* fn = which == 0 ? stage_kernel<0>(rmax) : which == 1 ? stage_kernel<1>(rmax)
+                   : which == 2 ? stage_kernel<2>(rmax) : stage_kernel<3>(rmax);
+    S2G_TRY(set_smem(fn, smem));
+    int budget = 0;  // DCT stages: blocks shared out by work (rows x length), as many as fit at once
+    if (which == 1 || which == 2) {
+        int occ = 0, dev = 0, nsm = 0;
+        S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 256, smem));
+        S2G_CUDA(cudaGetDevice(&dev));
+        S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        if (dct_ctas_per_sm > 0) occ = std::min(std::max(occ, 1), dct_ctas_per_sm);
+        budget = std::max(1, occ) * nsm;
+    }
+    // blocks of the longest transforms first: they take longest, and starting them first leaves
+    // the short classes' blocks for the tail of the launch
+    int order[kStageMaxClasses];
+    for (int c = 0; c < ncls; ++c) order[c] = c;
+    std::sort(order, order + ncls, [&](int x, int y) { return a.c[x].R > a.c[y].R; });
+    const StageArgs unsorted = a;
+    for (int c = 0; c < ncls; ++c) a.c[c] = unsorted.c[order[c]];
+    int blk = 0;
+    for (int c = 0; c < ncls; ++c) {
+        StageCls& k = a.c[c];
+        const int B = 16 * k.R, S = 2 * B;
+        long long nb;
+        if (which == 0 || which == 3) {
+            nb = (long long)k.N * (S / FftShape<1>::LAT);
+        } else {
+            const long long rows = (long long)k.N * B, most = (rows + FftShape<1>::W - 1) / FftShape<1>::W;
+            nb = std::llround(budget * ((double)k.N * B * k.R / wsum));
+            nb = std::max(1LL, std::min(nb, most));
+        }
+        if (blk + nb > INT_MAX / 2) return fail(S2G_ERR_UNSUPPORTED, "grouped stage too large");
+        k.blk0 = blk;
+        k.nblk = (int)nb;
+        blk += (int)nb;
+    }
+    static const char* names[4] = {"rows_fwd_f32_group", "dct_fwd_f32_group", "dct_inv_f32_group",
+                                   "rows_inv_f32_group"};
+    {
+        ProfScope ps_(names[which], st);
+        void* args[] = {&a};
+        S2G_CUDA(cudaLaunchKernel(fn, dim3(blk), dim3(256), args, smem, st));
+    }
+    return S2G_OK;
 }
 
 // Work counter of the contraction kernel: the int after the two intermediate arrays.

@@ -138,8 +138,8 @@ def test_group_tile_shapes_do_not_change_results():
     grid, rc, ic = _pack(g, ref)
     outs = []
     ncls = len(g.describe()["classes"])
-    for cps, tiles in [(0, None), (1, [32] * ncls), (2, [64] * ncls), (0, [16] * ncls)]:
-        g.set_tiles(cps, tiles)
+    for cps, tiles, dct in [(0, None, 0), (1, [32] * ncls, 1), (2, [64] * ncls, 2), (0, [16] * ncls, 3)]:
+        g.set_tiles(cps, tiles, dct)
         o_rc, o_ic, o_grid = torch.zeros_like(rc), torch.zeros_like(ic), torch.zeros_like(grid)
         g.fst_inv(grid, o_rc, o_ic, o_grid)
         g.sync_status()
@@ -149,7 +149,7 @@ def test_group_tile_shapes_do_not_change_results():
             assert torch.equal(a, b)
     g.autotune(force=True)
     t = g.describe()["tiles"]
-    assert set(t) == {"ctas_per_sm", "tile_n"}
+    assert set(t) == {"ctas_per_sm", "dct_ctas_per_sm", "tile_n"}
     o_rc, o_ic, o_grid = torch.zeros_like(rc), torch.zeros_like(ic), torch.zeros_like(grid)
     g.fst_inv(grid, o_rc, o_ic, o_grid)
     g.sync_status()
@@ -165,12 +165,28 @@ def test_group_graph_replay_counts_launches():
     g.fst(grid, rc, ic)
     torch.cuda.synchronize()
     nk = g.describe()["graph_kernels"][0]
-    assert nk == 3 * 2 + 1  # rows + DCT per class, one contraction
+    # every class here is in the short tier (bw <= 64): one rows-DFT, one DCT, one contraction
+    assert nk == 3
     lib = api.load()
     before = lib.s2g_launch_count()
     g.fst(grid, rc, ic)
     torch.cuda.synchronize()
     assert lib.s2g_launch_count() - before == nk
+
+
+def test_group_stage_launches_do_not_grow_with_classes():
+    """Five bandwidth classes in both tiers: a forward is one rows-DFT and one DCT launch per tier
+    and one contraction, five kernels, not two per class."""
+    torch = _torch()
+    g = api.Group([16, 32, 64, 128, 256, 256], api.PREC_FP16X2)
+    grid = torch.zeros(g.grid_total, dtype=torch.float32, device="cuda")
+    rc, ic = torch.zeros(g.coeff_total, device="cuda"), torch.zeros(g.coeff_total, device="cuda")
+    og = torch.zeros_like(grid)
+    g.fst(grid, rc, ic)
+    g.inv_fst(rc, ic, og)
+    torch.cuda.synchronize()
+    d = g.describe()
+    assert d["graph_kernels"][0] == 5 and d["graph_kernels"][1] == 5, d
 
 
 def test_group_rejects_bad_arguments():
