@@ -678,7 +678,7 @@ def group_bench(api, torch, stream, steps, warmup, seed):
     tiles = [t["tile_n"][str(c[0])] for c in d["classes"]]
     lib.s2g_prof_enable(1)
     for _ in range(5):
-        g.set_tiles(t["ctas_per_sm"], tiles, t["dct_ctas_per_sm"])
+        g.set_tiles(t["table_stages"], tiles, t["dct_ctas_per_sm"])
         g.fst_inv(grid, o_rc, o_ic, o_grid, stream)
     torch.cuda.synchronize()
     buf = ctypes.create_string_buffer(1 << 16)

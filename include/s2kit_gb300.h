@@ -308,15 +308,16 @@ int s2g_group_inv_fst(s2g_group group, const float* rcoeffs, const float* icoeff
 /* forward of grid into the coefficients, then inverse of those into grid_out, one graph */
 int s2g_group_fst_inv(s2g_group group, const float* grid, float* rcoeffs, float* icoeffs, float* grid_out,
                       void* stream);
-/* Times candidate shapes (N extent of each class's contraction tile, CTAs per SM of the
- * persistent contraction, resident blocks per SM the DCT stages are sized for) on the group's
+/* Times candidate shapes (N extent of each class's contraction tile, depth of the contraction's
+ * table-copy ring, resident blocks per SM the DCT stages are sized for) on the group's
  * whole forward + inverse sequence and keeps the fastest.  Results are cached per
  * (device, precision, class sizes); force != 0 re-measures.  $S2G_TUNE_CACHE, when set, names a
  * file that keeps them across processes.  Synchronous. */
 int s2g_group_autotune(s2g_group group, int force);
-/* Sets the shapes by hand: ctas_per_sm (0 = as many as fit) and one tile N per bandwidth class
+/* Sets the shapes by hand: table_stages (the contraction's table-copy ring depth: 0 = as many as
+ * fit, else 2..8) and one tile N per bandwidth class
  * in increasing bandwidth (0 = the class's whole table-row extent; NULL = all 0). */
-int s2g_group_set_tiles(s2g_group group, int ctas_per_sm, const int* tile_n);
+int s2g_group_set_tiles(s2g_group group, int table_stages, const int* tile_n);
 /* Sets the resident blocks per SM the grouped DCT stages are sized for (0 = as many as fit). */
 int s2g_group_set_dct_ctas(s2g_group group, int dct_ctas_per_sm);
 /* JSON description: classes [bw, count], chosen tiles, kernels per captured graph. */
@@ -331,12 +332,12 @@ int s2g_group_sync_status(s2g_group group);
  * of the six split products (1 = plain BF16 ... 6 = 3-term split).  Synchronous. */
 int s2g_selftest_tc(int N, int K, int nprod, const float* A, const float* B, float* D);
 
-/* Selects the tensor-core contraction kernel for later calls (process-wide): 1 (default) =
- * warp-specialised persistent kernel (scheduler/table-copy warp, MMA warp, A-producer warps,
- * epilogue warps; one CTA per SM) that moves its A operand -- and the inverse its output -- by
+/* Selects the tensor-core contraction's data path for later calls (process-wide): 1 (default) =
+ * the warp-specialised persistent kernel (scheduler/table-copy warp, MMA warp, A-producer warps,
+ * epilogue warps; one CTA per SM) moving its A operand -- and the inverse its output -- by
  * tensor-map TMA where it can (one bandwidth class, BF16 terms, bw >= 64); 2 = the same kernel
- * with per-thread asynchronous copies only; 0 = the kernel in which all threads stage each
- * chunk (two CTAs per SM).  All do the same arithmetic per work item and give identical results. */
+ * with per-thread asynchronous copies only.  Both do the same arithmetic per work item and give
+ * identical results. */
 int s2g_set_contraction_kernel(int which);
 
 /* Test hook for the failure path of the tensor-core contraction (off by default): with on != 0,

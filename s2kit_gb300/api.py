@@ -342,9 +342,9 @@ class Group:
     def autotune(self, force=False):
         check(self.lib.s2g_group_autotune(self.h, 1 if force else 0), "s2g_group_autotune")
 
-    def set_tiles(self, ctas_per_sm=0, tile_n=None, dct_ctas_per_sm=None):
+    def set_tiles(self, table_stages=0, tile_n=None, dct_ctas_per_sm=None):
         arr = None if tile_n is None else (C.c_int * len(tile_n))(*tile_n)
-        check(self.lib.s2g_group_set_tiles(self.h, ctas_per_sm, arr), "s2g_group_set_tiles")
+        check(self.lib.s2g_group_set_tiles(self.h, table_stages, arr), "s2g_group_set_tiles")
         if dct_ctas_per_sm is not None:
             check(self.lib.s2g_group_set_dct_ctas(self.h, dct_ctas_per_sm), "s2g_group_set_dct_ctas")
 

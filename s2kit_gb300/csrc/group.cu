@@ -16,8 +16,8 @@
 // parallel branches) and replayed on the caller's stream; the first call with a given set of
 // pointers runs eagerly and captures, later calls replay.
 //
-// Shapes (the N extent of each class's contraction tile, CTAs per SM of the persistent
-// contraction, resident blocks per SM the DCT stages are sized for) come from an autotuner that
+// Shapes (the N extent of each class's contraction tile, the depth of the contraction's table-copy
+// ring, resident blocks per SM the DCT stages are sized for) come from an autotuner that
 // times the group's whole forward + inverse sequence on its own sizes and keeps the fastest;
 // results are cached per (device, precision, class sizes) in memory and, when $S2G_TUNE_CACHE
 // names a file, on disk.
@@ -63,7 +63,7 @@ struct s2g_group_s {
     std::vector<s2g::GroupClass> cls;
     void* mem = nullptr;        // one device allocation: maps, intermediates, counters
     int* counters = nullptr;    // [0] forward, [1] inverse contraction work counters
-    int ctas_per_sm = 0;        // contraction: 0 = as many as fit
+    int table_stages = 0;       // contraction: table-copy ring depth, 0 = as many as fit
     int dct_ctas = 0;           // DCT stages: resident blocks per SM they are sized for, 0 = as many as fit
     cudaStream_t cap = nullptr;
     cudaStream_t side = nullptr;               // the short-transform tier's stream
@@ -129,7 +129,7 @@ static int group_fwd_seq(s2g_group g, const float* grid, float* rc, float* ic, c
         q.ic = ic;
         q.cmap = k.cmap;
     }
-    return split_leg(true, g->precision, spec, nc, g->counters, g->ctas_per_sm, st);
+    return split_leg(true, g->precision, spec, nc, g->counters, g->table_stages, st);
 }
 
 static int group_inv_seq(s2g_group g, const float* rc, const float* ic, float* grid, cudaStream_t st) {
@@ -147,7 +147,7 @@ static int group_inv_seq(s2g_group g, const float* rc, const float* ic, float* g
         q.F = k.buf0;
         q.cmap = k.cmap;
     }
-    S2G_TRY(split_leg(false, g->precision, spec, nc, g->counters + 1, g->ctas_per_sm, st));
+    S2G_TRY(split_leg(false, g->precision, spec, nc, g->counters + 1, g->table_stages, st));
     const int which[2] = {2, 3};  // Fc -> F -> grid
     return group_stages(
         g, which, 2, [&](int w, int c) -> const void* { return w == 0 ? g->cls[c].buf1 : g->cls[c].buf0; },
@@ -211,7 +211,7 @@ static bool g_tune_loaded = false;
 static std::string tune_key(s2g_group g) {
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, g->device);
-    std::string k = std::string(prop.name) + "|v2|p" + std::to_string(g->precision);
+    std::string k = std::string(prop.name) + "|v3|p" + std::to_string(g->precision);
     for (auto& c : g->cls) k += "|" + std::to_string(c.B) + "x" + std::to_string(c.N);
     for (auto& ch : k)
         if (ch == ' ') ch = '_';
@@ -248,7 +248,7 @@ static void tune_store(const std::string& key, const std::string& val) {
 }
 
 static std::string tune_value(s2g_group g) {
-    std::string v = std::to_string(g->ctas_per_sm) + " " + std::to_string(g->dct_ctas);
+    std::string v = std::to_string(g->table_stages) + " " + std::to_string(g->dct_ctas);
     for (auto& c : g->cls) v += " " + std::to_string(c.NB);
     return v;
 }
@@ -264,14 +264,14 @@ static bool tune_apply(s2g_group g, const std::string& v) {
         p = end;
     }
     if (x.size() != g->cls.size() + 2) return false;
-    g->ctas_per_sm = x[0];
+    g->table_stages = x[0];
     g->dct_ctas = x[1];
     for (size_t c = 0; c < g->cls.size(); ++c) g->cls[c].NB = x[c + 2];
     return true;
 }
 
 static void tune_describe(s2g_group g) {
-    std::string d = "{\"ctas_per_sm\": " + std::to_string(g->ctas_per_sm) +
+    std::string d = "{\"table_stages\": " + std::to_string(g->table_stages) +
                     ", \"dct_ctas_per_sm\": " + std::to_string(g->dct_ctas) + ", \"tile_n\": {";
     for (size_t c = 0; c < g->cls.size(); ++c) {
         if (c) d += ", ";
@@ -334,7 +334,7 @@ static int group_autotune(s2g_group g, int force) {
     S2G_CUDA(cudaMemsetAsync(rc, 0, sizeof(float) * nbuf, g->cap));
     int r = S2G_OK;
     float best = 0;
-    g->ctas_per_sm = 0;
+    g->table_stages = 0;
     g->dct_ctas = 0;
     for (auto& c : g->cls) c.NB = 0;
     auto timed = [&](float* ms) { return time_group(g, grid, rc, ic, grid_out, 3, ms); };
@@ -361,14 +361,14 @@ static int group_autotune(s2g_group g, int force) {
         }
         c.NB = keep;
     }
-    for (int cps : {1, 2, 3}) {
+    for (int ts : {2, 3, 4, 6}) {
         if (r != S2G_OK) break;
-        const int keep = g->ctas_per_sm;
-        g->ctas_per_sm = cps;
+        const int keep = g->table_stages;
+        g->table_stages = ts;
         float ms = 0;
         r = timed(&ms);
         if (r == S2G_OK && ms < best * 0.98f) best = ms;
-        else g->ctas_per_sm = keep;
+        else g->table_stages = keep;
     }
     for (int dc : {1, 2, 3, 4}) {
         if (r != S2G_OK) break;
@@ -556,13 +556,14 @@ int s2g_group_autotune(s2g_group g, int force) {
     return group_autotune(g, force);
 }
 
-int s2g_group_set_tiles(s2g_group g, int ctas_per_sm, const int* tile_n) {
+int s2g_group_set_tiles(s2g_group g, int table_stages, const int* tile_n) {
     S2G_TRY(group_check(g));
-    if (ctas_per_sm < 0 || ctas_per_sm > 8) return fail(S2G_ERR_ARG, "ctas_per_sm %d outside [0, 8]", ctas_per_sm);
+    if (table_stages < 0 || table_stages == 1 || table_stages > 8)
+        return fail(S2G_ERR_ARG, "table_stages %d: 0 or 2..8", table_stages);
     for (size_t c = 0; tile_n && c < g->cls.size(); ++c)
         if (tile_n[c] < 0 || tile_n[c] > 256 || tile_n[c] % 16)
             return fail(S2G_ERR_ARG, "tile_n[%zu] = %d: a multiple of 16 in [0, 256]", c, tile_n[c]);
-    g->ctas_per_sm = ctas_per_sm;
+    g->table_stages = table_stages;
     for (size_t c = 0; c < g->cls.size(); ++c) g->cls[c].NB = tile_n ? tile_n[c] : 0;
     for (auto& gr : g->graphs) drop_graph(gr);
     tune_describe(g);

@@ -186,8 +186,8 @@ struct LegSpec {
     const int64_t* cmap;      // function -> coefficient offset (null: f * B * B)
 };
 // One persistent launch over every class; counter: one device int (zeroed on `st` here);
-// ctas_per_sm 0 = as many as fit.
-int split_leg(bool fwd, int precision, const LegSpec* cls, int ncls, int* counter, int ctas_per_sm,
+// table_stages: depth of the kernel's table-copy ring, 0 = as many stages as fit.
+int split_leg(bool fwd, int precision, const LegSpec* cls, int ncls, int* counter, int table_stages,
               cudaStream_t st);
 // Packs the tensor-core operands of `t` for `precision` now (they are otherwise packed on first use).
 int split_prepare(Tables* t, int precision);

@@ -1022,7 +1022,7 @@ struct Leg {
 __constant__ int c_prod_a[6] = {0, 0, 1, 0, 1, 2};
 __constant__ int c_prod_b[6] = {0, 1, 0, 2, 1, 0};
 
-static constexpr int kTPB = 256;
+static constexpr int kTPB = 256;  // A-producer threads: two (row, 8-column segment) tasks each
 static constexpr uint32_t kATile = 128u * kKC * 2u;  // bytes of one A term tile
 static constexpr uint32_t kSBO = (kKC / 8) * 128;    // byte stride of 8-row groups in a tile
 
@@ -1235,195 +1235,9 @@ __device__ __forceinline__ void issue_table(uint8_t* sb, const uint8_t* blob, in
     for (int s = 0; s < NT; ++s) tc::bulk_g2s(sb + s * part, src + (size_t)s * tile, part, bar);
 }
 
-template <bool FWD, bool F16>
-__global__ void __launch_bounds__(kTPB, 2) k_leg_tc(Leg p, uint32_t stage_bytes, uint32_t ncols) {
-    constexpr int NT = F16 ? 2 : 3;
-    extern __shared__ __align__(1024) uint8_t dsm[];
-    uint8_t* smem = (uint8_t*)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
-    __shared__ uint64_t bars[4];  // [0,1] table bytes landed, [2,3] MMAs of the stage done
-    __shared__ uint32_t tmem_slot;
-    __shared__ int s_abort;
-    __shared__ int s_dec[6];  // decoded item: class, m, t, sub-block, latitude block, first function
-    __shared__ float s_rinv[128];  // per-row inverse scale (FP16 terms)
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < 4; ++i) tc::mbar_init(&bars[i], 1);
-        tc::fence_mbar_init();
-        s_abort = 0;
-    }
-    // two accumulators per item: columns [0, NB) take the leading product x0*t0, [ncols/2,
-    // ncols/2 + NB) the correction products; each FP32 accumulation step in TMEM truncates
-    // relative to the accumulator's own magnitude, so the small terms are not rounded against
-    // the large sum
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
-    tc::tc_fence_before();
-    __syncthreads();
-    tc::tc_fence_after();
-    const uint32_t tmem = tmem_slot, corr = ncols / 2;
-    uint32_t gc = 0;  // chunks this CTA has processed: stage gc & 1, barrier phase (gc >> 1) & 1
-    // next work item (thread 0): fetched one item ahead, during the previous item's epilogue
-    long long item = threadIdx.x == 0 ? (long long)atomicAdd(p.counter, 1) : 0;
-
-    for (;;) {
-        __syncthreads();  // the previous item's epilogue has finished with shared memory
-        if (threadIdx.x == 0) {
-            // decode: class, then (64-function tile, order m, latitude block nb, sub-block, parity t);
-            // parity is the fastest index, so the two items that write the interleaved (stride-2)
-            // halves of the same coefficient rows run back to back and their sectors merge in L2
-            if (item >= p.nitems) {
-                s_dec[0] = -1;
-            } else {
-                int ci = 0;
-                while (ci + 1 < p.ncls && item >= p.cls[ci + 1].item0) ++ci;
-                const LegClass& K = p.cls[ci];
-                const long long li = item - K.item0;
-                const int rem = (int)(li % K.per_tile);
-                const int2 mj = K.itab[rem];
-                const int lo = mj.x, j = mj.y;
-                const int nsub = (geo(FWD, K.B, lo).NP + K.NB - 1) / K.NB;
-                s_dec[0] = ci;
-                s_dec[1] = lo;
-                s_dec[2] = j & 1;
-                s_dec[3] = (j >> 1) % nsub;
-                s_dec[4] = (j >> 1) / nsub;
-                s_dec[5] = (int)(li / K.per_tile) * 64;
-            }
-        }
-        __syncthreads();
-        if (s_dec[0] < 0 || s_abort) break;
-        const LegClass K = p.cls[s_dec[0]];  // by value: registers, not parameter-space loads in the loops
-        const int m = s_dec[1], t = s_dec[2], sub = s_dec[3], nb = s_dec[4], f0 = s_dec[5];
-        const int B = K.B;
-        const Geo g = geo(FWD, B, m);
-        const int n0 = sub * K.NB;
-        const int rows = min(K.NB, g.NP - n0);
-        const bool nv = naive_order(m);
-        const int nchunks = g.nch;
-        const uint8_t* blob = K.blob + K.blob_off[m] + (size_t)(t * g.nblk + nb) * nchunks * NT * g.NP * kKC * 2;
-        const uint32_t idesc = F16 ? tc::idesc_f16_f32(128, rows) : tc::idesc_bf16_f32(128, rows);
-
-        // Table chunks 0 and 1 are issued here (every MMA of the previous item has retired);
-        // chunk c+1 right after the MMAs of chunk c, once those of chunk c-1 have retired.
-        if (threadIdx.x == 0) {
-            for (int c = 0; c < 2 && c < nchunks; ++c) {
-                const uint32_t s = (gc + c) & 1;
-                issue_table<F16>(smem + s * stage_bytes + NT * kATile, blob, g.NP, n0, rows, c, &bars[s]);
-            }
-        }
-        float va[kTasks][8];
-        float sc[kTasks];
-        if (F16) {
-            // row scales: largest magnitude of each row over all chunks; the pass runs from the
-            // last chunk down, so chunk 0 is left in registers for the main loop
-            float mx[kTasks];
-#pragma unroll
-            for (int q = 0; q < kTasks; ++q) mx[q] = 0.f;
-            for (int c = nchunks - 1; c >= 0; --c) {
-                load_a<FWD>(K, m, nv, t, f0, c, va, threadIdx.x);
-#pragma unroll
-                for (int q = 0; q < kTasks; ++q)
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) mx[q] = fmaxf(mx[q], fabsf(va[q][e]));
-            }
-#pragma unroll
-            for (int q = 0; q < kTasks; ++q) {
-                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 8));
-                mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], 16));
-                int e = 0;
-                frexpf(mx[q], &e);  // mx < 2^e
-                const int sh = mx[q] > 0.f ? min(14 - e, 120) : 0;
-                sc[q] = ldexpf(1.f, sh);
-                int r, seg;
-                task_rs(threadIdx.x, q, r, seg);
-                if (seg == 0) s_rinv[r] = ldexpf(1.f, -sh);
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < kTasks; ++q) sc[q] = 1.f;
-            load_a<FWD>(K, m, nv, t, f0, 0, va, threadIdx.x);
-        }
-        for (int c = 0; c < nchunks; ++c) {
-            const uint32_t gcc = gc + c;
-            const uint32_t s = gcc & 1;
-            uint8_t* st = smem + s * stage_bytes;
-            // the A part of stage s was last read by the MMAs of chunk gcc-2, which have retired
-            __syncthreads();
-            if (s_abort) break;
-            store_a<F16>(st, va, sc, threadIdx.x);
-            if (c + 1 < nchunks) load_a<FWD>(K, m, nv, t, f0, c + 1, va, threadIdx.x);  // in flight across the MMA issue
-            tc::fence_proxy_async_smem();
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                if (!tc::mbar_wait(&bars[s], (gcc >> 1) & 1)) {
-                    s_abort = 1;
-                } else {
-                    tc::tc_fence_after();
-                    const uint32_t sa = tc::smem_u32(st), sb = tc::smem_u32(st + NT * kATile);
-                    const uint32_t bpart = (uint32_t)rows * kKC * 2;
-                    for (int ks = 0; ks < kKC / 16; ++ks) {
-                        for (int pr = 0; pr < p.nprod; ++pr) {
-                            const uint64_t da = tc::sdesc(sa + c_prod_a[pr] * kATile + ks * 256, 128, kSBO);
-                            const uint64_t db = tc::sdesc(sb + c_prod_b[pr] * bpart + ks * 256, 128, kSBO);
-                            const bool first = (c == 0 && ks == 0 && pr <= 1);  // first write of an accumulator
-                            tc::mma_bf16(tmem + (pr ? corr : 0u), da, db, idesc, first ? 0u : 1u);
-                        }
-                    }
-                    tc::mma_commit(&bars[2 + s]);
-                    if (c + 1 < nchunks && c >= 1) {
-                        if (!tc::mbar_wait(&bars[2 + (s ^ 1)], ((gcc - 1) >> 1) & 1)) {
-                            s_abort = 1;
-                        } else {
-                            uint8_t* sn = smem + (s ^ 1) * stage_bytes + NT * kATile;
-                            issue_table<F16>(sn, blob, g.NP, n0, rows, c + 1, &bars[s ^ 1]);
-                        }
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && !s_abort) {
-            const uint32_t gl = gc + nchunks - 1;
-            if (!tc::mbar_wait(&bars[2 + (gl & 1)], (gl >> 1) & 1)) s_abort = 1;
-        }
-        gc += nchunks;
-        if (threadIdx.x == 0) item = atomicAdd(p.counter, 1);  // overlaps the epilogue
-        __syncthreads();
-        if (s_abort) break;
-        // Epilogue: TMEM -> registers (warps 0-3, one accumulator row per thread) -> padded smem
-        // tile D[r][i] (the stage buffers are free: all copies and MMAs of this item are done)
-        // -> all 8 warps write the outputs with consecutive threads on consecutive columns.
-        float* dt = reinterpret_cast<float*>(smem);
-        const int DS = rows + 1;  // odd row stride
-        if (warp < 4) {
-            tc::tc_fence_after();
-            const int r = warp * 32 + lane;
-            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-            const float rs = F16 ? s_rinv[r] * K.tab_inv : 1.f;
-            for (int cb = 0; cb < rows; cb += 16) {
-                float v[16];
-                ld_sum(trow + cb, corr, p.nprod > 1, v);
-#pragma unroll
-                for (int q = 0; q < 16; ++q) dt[r * DS + cb + q] = v[q] * rs;
-            }
-            tc::tc_fence_before();
-        }
-        __syncthreads();
-        epi_store<FWD>(K, m, t, nb, g.NP, f0, n0, rows, dt, DS, warp, kTPB / 32, lane);
-    }
-    if (s_abort && threadIdx.x == 0) atomicExch(p.err, S2G_ERR_TIMEOUT);
-    tc::tc_fence_before();
-    __syncthreads();
-    if (warp == 0) {
-        tc::tc_fence_after();
-        tc::tmem_dealloc(tmem, ncols);
-    }
-}
-
 // ------------------------------------------------------------------------------------
-// Warp-specialised form of the contraction: the same work items and the same arithmetic per
-// item as k_leg_tc (results are bit-identical), with the stages of consecutive items
-// overlapped.  16 warps, one CTA per SM:
+// Warp-specialised contraction: the stages of consecutive work items overlapped.  16 warps, one
+// CTA per SM:
 //   warp 0     : scheduler (fetches and decodes items into a kNI-entry ring in shared memory)
 //                and table producer (bulk copies into an nbs-stage ring);
 //   warp 1     : MMA issuer (one thread; two accumulator pairs in TMEM when they fit, so the
@@ -1451,6 +1265,51 @@ static constexpr uint32_t kStgBytes = kAProd * kTasks * 8 * sizeof(float);  // o
 struct WsItem {
     int ci, m, t, sub, nb, f0;
 };
+
+// The K chunks an item multiplies, [c0, c1), and per chunk the N rows [r0, r0 + n) its MMAs cover.
+// The seminaive table of order m is zero where the cosine frequency index j exceeds m/2 + i, i the
+// degree index (tz above; seminaive.c:183-197 stops each degree's sum at its last frequency): the
+// forward's row i (N = degrees) has non-zero entries only in chunks up to (m/2 + i) / 32, the
+// inverse's row j (N = frequencies) only from chunk (j - m/2) / 32 on.  Chunks no row of the item
+// reaches are skipped (no A or table load, no MMA), and within a chunk the MMAs leave out the
+// 16-row blocks that are zero there.  The first chunk of an item covers every row, since it
+// starts the accumulators; skipped products are exact zeros, so the sums do not change.  Naive
+// orders are dense.
+struct Span {
+    int c0, c1;
+};
+
+__device__ __forceinline__ Span item_span(bool fwd, int nch, int m, int n0, int rows) {
+    if (naive_order(m)) return Span{0, nch};
+    const int h = m / 2;
+    if (fwd) return Span{0, min(nch, (h + n0 + rows - 1) / kKC + 1)};
+    const int lo = n0 - h - (kKC - 1);  // the first chunk c with h + 32 c + 31 >= n0
+    return Span{lo > 0 ? (lo + kKC - 1) / kKC : 0, nch};
+}
+
+template <bool FWD>
+__device__ __forceinline__ Span item_span(const Leg& p, const WsItem& e) {
+    const LegClass& K = p.cls[e.ci];
+    const Geo g = geo(FWD, K.B, e.m);
+    const int n0 = e.sub * K.NB;
+    return item_span(FWD, g.nch, e.m, n0, min(K.NB, g.NP - n0));
+}
+
+// Rows of chunk c's MMAs: r0 (a multiple of 16) and the count n, within the item's `rows`.
+__device__ __forceinline__ void chunk_rows(bool fwd, int m, int n0, int rows, int c, bool first, int& r0, int& n) {
+    r0 = 0;
+    n = rows;
+    if (first || naive_order(m)) return;
+    const int h = m / 2;
+    if (fwd) {
+        const int z = kKC * c - h - n0;  // rows below z (item-relative) are zero in chunk c
+        r0 = z > 0 ? (z & ~15) : 0;
+        n = rows - r0;
+    } else {
+        const int last = h + kKC * c + kKC - n0;  // rows at or above `last` are zero in chunk c
+        n = min(rows, (last + 15) & ~15);
+    }
+}
 
 template <bool FWD>
 __device__ __forceinline__ WsItem decode_item(const Leg& p, long long item) {
@@ -1552,8 +1411,9 @@ __device__ __forceinline__ void produce_a_async(const Leg& p, uint8_t* smem, flo
                     break;
                 }
                 have_ei = true;
-                ci = 0;
-                nch_i = geo(FWD, p.cls[ei.ci].B, ei.m).nch;
+                const Span sp = item_span<FWD>(p, ei);
+                ci = sp.c0;
+                nch_i = sp.c1;
             }
             issue_chunk<FWD>(p.cls[ei.ci], ei, ci, stg, (int)(n_iss % (uint32_t)nstg), tid);
             tc::cp_async_commit();
@@ -1574,9 +1434,9 @@ __device__ __forceinline__ void produce_a_async(const Leg& p, uint8_t* smem, flo
         const WsItem e = items[slot];
         tc::mbar_arrive(&item_empty[slot]);
         if (e.ci < 0) break;
-        const int nch = geo(FWD, p.cls[e.ci].B, e.m).nch;
+        const Span sp = item_span<FWD>(p, e);
         bool ok = true;
-        for (int c = 0; c < nch; ++c, ++ac) {
+        for (int c = sp.c0; c < sp.c1; ++c, ++ac) {
             // chunk (k, c) is the oldest one issued: the issue cursor never falls behind
             if (!top_up() || n_iss == n_con) {
                 ok = false;
@@ -1609,6 +1469,22 @@ __device__ __forceinline__ void produce_a_async(const Leg& p, uint8_t* smem, flo
     tc::cp_async_wait(0);  // no copy lands in shared memory after this role has left
 }
 
+// v[x] = w[u + 2x], x < 8, for a run-time u in [0, 4] (one unrolled copy per u, no local memory).
+template <int U>
+__device__ __forceinline__ void pick_u(const float (&w)[20], float* v) {
+#pragma unroll
+    for (int x = 0; x < 8; ++x) v[x] = w[U + 2 * x];
+}
+__device__ __forceinline__ void pick_stride2(const float (&w)[20], int u, float* v) {
+    switch (u) {
+        case 0: pick_u<0>(w, v); break;
+        case 1: pick_u<1>(w, v); break;
+        case 2: pick_u<2>(w, v); break;
+        case 3: pick_u<3>(w, v); break;
+        default: pick_u<4>(w, v); break;
+    }
+}
+
 // BF16 A producers fed by tensor-map TMA: the scheduler warp loads each chunk's A operand
 // (FP32) into a staging ring; the producers split their two tasks' values into BF16 terms.
 template <bool FWD>
@@ -1636,10 +1512,10 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
         const LegClass& K = p.cls[e.ci];
         const int B = K.B, m = e.m, t = e.t;
         const bool nv = FWD && naive_order(m);
-        const int nch = geo(FWD, B, m).nch;
+        const Span sp = item_span<FWD>(p, e);
         const int base = FWD ? 0 : index_of_harmonic_coeff(m, m, B);
         bool ok = true;
-        for (int c = 0; c < nch; ++c, ++ac, ++sc) {
+        for (int c = sp.c0; c < sp.c1; ++c, ++ac, ++sc) {
             if (!tc::mbar_wait(&stg_full[ss], sph)) {
                 ok = false;
                 break;
@@ -1662,16 +1538,26 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
                     va[q][6] = valid ? b.z : 0.f, va[q][7] = valid ? b.w : 0.f;
                 } else {
                     // planes [p][64 functions][kInvBox]; the box starts at the 16-byte aligned element
-                    // at or below the chunk's first coefficient base + 64 c
+                    // at or below the chunk's first coefficient base + 64 c.  The task's eight
+                    // stride-2 values lie in the 20 floats from 16 seg on, read as five aligned
+                    // float4: a quarter-warp's eight rows then fall in eight distinct 16-byte bank
+                    // groups (rows are 272 bytes apart), where scalar reads of the same values
+                    // collided four ways (the segments 0 and 2, 1 and 3 of a row share banks)
                     const int o = (base + c * 64) & 3;
-                    const float* row = reinterpret_cast<const float*>(sb) + (r >> 6) * (64 * kInvBox) +
-                                       (r & 63) * kInvBox + o;
+                    const float4* row4 = reinterpret_cast<const float4*>(
+                        reinterpret_cast<const float*>(sb) + (r >> 6) * (64 * kInvBox) + (r & 63) * kInvBox +
+                        16 * seg);
+                    float w[20];
+#pragma unroll
+                    for (int k4 = 0; k4 < 5; ++k4) {
+                        const float4 f4 = row4[k4];
+                        w[4 * k4] = f4.x, w[4 * k4 + 1] = f4.y, w[4 * k4 + 2] = f4.z, w[4 * k4 + 3] = f4.w;
+                    }
+                    pick_stride2(w, o + t, va[q]);
                     const int lim = B - m - c * 64;
 #pragma unroll
-                    for (int x = 0; x < 8; ++x) {
-                        const int d = 2 * (seg * 8 + x) + t;
-                        va[q][x] = d < lim ? row[d] : 0.f;
-                    }
+                    for (int x = 0; x < 8; ++x)
+                        if (2 * (seg * 8 + x) + t >= lim) va[q][x] = 0.f;
                 }
             }
             // the next chunk's TMA (async proxy) overwrites this staging buffer once the release
@@ -1814,7 +1700,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 const int n0 = e.sub * K.NB, rows = min(K.NB, g.NP - n0);
                 const uint8_t* blob =
                     K.blob + K.blob_off[e.m] + (size_t)(e.t * g.nblk + e.nb) * g.nch * NT * g.NP * kKC * 2;
-                for (int c = 0; c < g.nch; ++c, ++bc) {
+                const Span sp = item_span(FWD, g.nch, e.m, n0, rows);
+                for (int c = sp.c0; c < sp.c1; ++c, ++bc) {
                     if (!tc::mbar_wait(&b_empty[bs], bph ^ 1)) {
                         s_abort = 1;
                         break;
@@ -1845,8 +1732,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 const WsItem e = items[slot];
                 tc::mbar_arrive(&item_empty[slot]);
                 if (e.ci < 0) break;
-                const int nch = geo(FWD, p.cls[e.ci].B, e.m).nch;
-                for (int c = 0; c < nch; ++c, ++stc) {
+                const Span sp = item_span<FWD>(p, e);
+                for (int c = sp.c0; c < sp.c1; ++c, ++stc) {
                     if (!tc::mbar_wait(&stg_empty[ss], sph ^ 1)) {
                         s_abort = 1;
                         break;
@@ -1878,8 +1765,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 if (e.ci < 0) break;
                 const LegClass& K = p.cls[e.ci];
                 const Geo g = geo(FWD, K.B, e.m);
-                const int rows = min(K.NB, g.NP - e.sub * K.NB);
-                const uint32_t idesc = F16 ? tc::idesc_f16_f32(128, rows) : tc::idesc_bf16_f32(128, rows);
+                const int n0 = e.sub * K.NB, rows = min(K.NB, g.NP - n0);
+                const Span sp = item_span(FWD, g.nch, e.m, n0, rows);
                 const uint32_t bpart = (uint32_t)rows * kKC * 2;
                 const int buf = k % nacc;
                 if (!tc::mbar_wait(&acc_empty[buf], ((k / nacc) & 1) ^ 1)) {
@@ -1889,7 +1776,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 tc::tc_fence_after();
                 const uint32_t d0 = tmem + buf * accw;
                 bool ok = true;
-                for (int c = 0; c < g.nch; ++c, ++ac) {
+                for (int c = sp.c0; c < sp.c1; ++c, ++ac) {
                     const int sa = ac % kNAS;
                     if (!tc::mbar_wait(&a_full[sa], (ac / kNAS) & 1) || !tc::mbar_wait(&b_full[sb], bph)) {
                         ok = false;
@@ -1902,14 +1789,21 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                     // unrolled for the 6- and 3-product modes, and the operand descriptors are the
                     // chunk's base descriptors plus constant offsets (start address >> 4 in bits 0-13;
                     // shared-memory addresses stay below 2^18, so the sums do not carry)
-                    const uint64_t da0 = tc::sdesc(sa_addr, 128, kSBO), db0 = tc::sdesc(sb_addr, 128, kSBO);
+                    // rows [r0, r0 + nr) of this chunk: D columns and table rows offset by r0 (a table
+                    // row is 64 bytes of the K-major core-matrix layout, 4 descriptor units)
+                    int r0, nr;
+                    chunk_rows(FWD, e.m, n0, rows, c, c == sp.c0, r0, nr);
+                    const uint32_t idesc = F16 ? tc::idesc_f16_f32(128, nr) : tc::idesc_bf16_f32(128, nr);
+                    const uint64_t da0 = tc::sdesc(sa_addr, 128, kSBO),
+                                   db0 = tc::sdesc(sb_addr, 128, kSBO) + (uint64_t)(4 * r0);
                     const uint64_t bstep = bpart >> 4;
+                    const uint32_t dr = d0 + (uint32_t)r0;
                     if (p.nprod == 6)
-                        mma_chunk<6>(d0, corr, da0, db0, bstep, idesc, c == 0);
+                        mma_chunk<6>(dr, corr, da0, db0, bstep, idesc, c == sp.c0);
                     else if (p.nprod == 3)
-                        mma_chunk<3>(d0, corr, da0, db0, bstep, idesc, c == 0);
+                        mma_chunk<3>(dr, corr, da0, db0, bstep, idesc, c == sp.c0);
                     else
-                        mma_chunk<1>(d0, corr, da0, db0, bstep, idesc, c == 0);
+                        mma_chunk<1>(dr, corr, da0, db0, bstep, idesc, c == sp.c0);
                     tc::mma_commit(&a_empty[sa]);
                     tc::mma_commit(&b_empty[sb]);
                     if (++sb == nbs) {
@@ -2112,10 +2006,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             } else {
 #pragma unroll
                 for (int q = 0; q < kTasks; ++q) sc[q] = 1.f;
-                load_a<FWD>(K, m, nv, t, f0, 0, va, tid);
             }
+            const Span sp = item_span<FWD>(p, e);
+            load_a<FWD>(K, m, nv, t, f0, sp.c0, va, tid);
             bool ok = true;
-            for (int c = 0; c < g.nch; ++c, ++ac) {
+            for (int c = sp.c0; c < sp.c1; ++c, ++ac) {
                 const int s = ac % kNAS;
                 if (!tc::mbar_wait(&a_empty[s], ((ac / kNAS) & 1) ^ 1)) {
                     ok = false;
@@ -2124,7 +2019,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 store_a<F16>(smem + s * kAStage, va, sc, tid);
                 tc::fence_proxy_async_smem();
                 tc::mbar_arrive(&a_full[s]);
-                if (c + 1 < g.nch) load_a<FWD>(K, m, nv, t, f0, c + 1, va, tid);
+                if (c + 1 < sp.c1) load_a<FWD>(K, m, nv, t, f0, c + 1, va, tid);
             }
             if (!ok) {
                 s_abort = 1;
@@ -2162,26 +2057,11 @@ static int check_prec(int precision, int* nprod, bool* f16) {
     return S2G_OK;
 }
 
-// Resident CTAs per SM of a contraction kernel at a shared-memory size (cached).
-static int leg_occupancy(const void* fn, size_t smem, int* occ) {
-    static std::mutex mu;
-    static std::vector<std::pair<std::pair<const void*, size_t>, int>> cache;
-    std::lock_guard<std::mutex> lk(mu);
-    for (auto& e : cache)
-        if (e.first.first == fn && e.first.second == smem) return (*occ = e.second), S2G_OK;
-    int v = 0;
-    S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, fn, kTPB, smem));
-    cache.push_back({{fn, smem}, v});
-    *occ = v;
-    return S2G_OK;
-}
-
-// Contraction kernel: 0 = k_leg_tc (all threads load, split and stage each chunk; two CTAs
-// per SM), 1 = k_leg_ws (warp-specialised, one CTA per SM).
-static std::atomic<int> g_leg_kernel{1};
 static std::atomic<int> g_leg_stall{0};  // test hook, see s2g_test_stall_contraction
 
-static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items, int* counter, cudaStream_t st) {
+// table_stages: the depth of the table-copy ring (0: as many stages as fit, up to kMaxNBS).
+static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items, int* counter, int table_stages,
+                         cudaStream_t st) {
     const void* fn = fwd ? (f16 ? (const void*)k_leg_ws<true, true> : (const void*)k_leg_ws<true, false>)
                          : (f16 ? (const void*)k_leg_ws<false, true> : (const void*)k_leg_ws<false, false>);
     const int nt = f16 ? 2 : 3;
@@ -2228,7 +2108,7 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
         if (nbs_fit >= 2 || nstg <= nstg_min || f16) break;
         --nstg;
     }
-    const int nbs = (int)std::min<long long>(kMaxNBS, nbs_fit);
+    const int nbs = (int)std::min<long long>(table_stages > 0 ? std::min(table_stages, kMaxNBS) : kMaxNBS, nbs_fit);
     if (nbs < 2) return fail(S2G_ERR_UNSUPPORTED, "warp-specialised contraction does not fit in shared memory");
     const size_t stg_bytes = (size_t)nstg * stg_stride;
     const size_t smem = 1024 + a_bytes + stg_bytes + (size_t)nbs * b_stage + epi;
@@ -2337,7 +2217,7 @@ static int get_itab(Split* s, bool fwd, int NB, const int2** out, int* per_tile)
     return S2G_OK;
 }
 
-int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* counter, int ctas_per_sm,
+int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* counter, int table_stages,
               cudaStream_t st) {
     int nprod = 0;
     bool f16 = false;
@@ -2351,7 +2231,7 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     long long items = 0;
     int nbmax = 16;
     // tensor-map TMA path: one class, BF16 terms, contiguous batches, bw >= 64, warp-specialised kernel
-    const bool want_tma = g_leg_tma && g_leg_kernel == 1 && !f16 && ncls == 1 && !spec[0].cmap &&
+    const bool want_tma = g_leg_tma && !f16 && ncls == 1 && !spec[0].cmap &&
                           spec[0].t->bw >= 64;
     for (int c = 0; c < ncls; ++c) {
         const LegSpec& q = spec[c];
@@ -2389,34 +2269,7 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     if (items == 0) return S2G_OK;
     p.tma = want_tma && setup_tma(p, fwd, spec[0]) ? 1 : 0;
     if (items > 0x7fffffffLL) return fail(S2G_ERR_ARG, "contraction of %lld work items is too large", items);
-    const int nt = f16 ? 2 : 3;
-    if (g_leg_kernel == 1) return launch_leg_ws(fwd, f16, p, nbmax, items, counter, st);
-    const size_t stage = (size_t)nt * kATile + (size_t)nt * nbmax * kKC * 2;
-    const size_t epi = (size_t)128 * (nbmax + 1) * sizeof(float);
-    const size_t smem = 1024 + std::max(2 * stage, epi);
-    uint32_t ncols = 32;
-    while (ncols < 2u * nbmax) ncols <<= 1;
-    const void* fn = fwd ? (f16 ? (const void*)k_leg_tc<true, true> : (const void*)k_leg_tc<true, false>)
-                         : (f16 ? (const void*)k_leg_tc<false, true> : (const void*)k_leg_tc<false, false>);
-    S2G_TRY(set_smem(fn, smem));
-    int occ = 0, dev = 0, nsm = 0;
-    S2G_TRY(leg_occupancy(fn, smem, &occ));
-    S2G_CUDA(cudaGetDevice(&dev));
-    S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    occ = std::min(occ, (int)(512 / ncols));  // every resident CTA holds its TMEM columns
-    if (ctas_per_sm > 0) occ = std::min(occ, ctas_per_sm);
-    if (occ < 1) return fail(S2G_ERR_UNSUPPORTED, "contraction kernel does not fit on an SM (%zu B smem)", smem);
-    const int grid = (int)std::min<long long>(items, (long long)occ * nsm);
-    S2G_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
-    {
-        ProfScope ps_(fwd ? "leg_tc_fwd" : "leg_tc_inv", st);
-        if (fwd && f16) k_leg_tc<true, true><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
-        else if (fwd) k_leg_tc<true, false><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
-        else if (f16) k_leg_tc<false, true><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
-        else k_leg_tc<false, false><<<grid, kTPB, smem, st>>>(p, (uint32_t)stage, ncols);
-    }
-    S2G_CUDA(cudaGetLastError());
-    return S2G_OK;
+    return launch_leg_ws(fwd, f16, p, nbmax, items, counter, table_stages, st);
 }
 
 // Grid of a persistent kernel: the CTAs that fit on the GPU at once (cached per kernel and
@@ -2915,8 +2768,7 @@ extern "C" int s2g_test_stall_contraction(int on) {
 }
 
 extern "C" int s2g_set_contraction_kernel(int which) {
-    if (which < 0 || which > 2) return s2g::fail(S2G_ERR_ARG, "contraction kernel %d (0, 1 or 2)", which);
-    s2g::g_leg_kernel = which == 0 ? 0 : 1;
+    if (which < 1 || which > 2) return s2g::fail(S2G_ERR_ARG, "contraction data path %d (1 or 2)", which);
     s2g::g_leg_tma = which == 1 ? 1 : 0;
     return S2G_OK;
 }

@@ -138,8 +138,8 @@ def test_group_tile_shapes_do_not_change_results():
     grid, rc, ic = _pack(g, ref)
     outs = []
     ncls = len(g.describe()["classes"])
-    for cps, tiles, dct in [(0, None, 0), (1, [32] * ncls, 1), (2, [64] * ncls, 2), (0, [16] * ncls, 3)]:
-        g.set_tiles(cps, tiles, dct)
+    for ts, tiles, dct in [(0, None, 0), (2, [32] * ncls, 1), (3, [64] * ncls, 2), (0, [16] * ncls, 3)]:
+        g.set_tiles(ts, tiles, dct)
         o_rc, o_ic, o_grid = torch.zeros_like(rc), torch.zeros_like(ic), torch.zeros_like(grid)
         g.fst_inv(grid, o_rc, o_ic, o_grid)
         g.sync_status()
@@ -149,7 +149,7 @@ def test_group_tile_shapes_do_not_change_results():
             assert torch.equal(a, b)
     g.autotune(force=True)
     t = g.describe()["tiles"]
-    assert set(t) == {"ctas_per_sm", "dct_ctas_per_sm", "tile_n"}
+    assert set(t) == {"table_stages", "dct_ctas_per_sm", "tile_n"}
     o_rc, o_ic, o_grid = torch.zeros_like(rc), torch.zeros_like(ic), torch.zeros_like(grid)
     g.fst_inv(grid, o_rc, o_ic, o_grid)
     g.sync_status()

@@ -224,8 +224,8 @@ def test_split_rejects_unsupported():
 @pytest.mark.parametrize("bw,nb", [(16, 70), (64, 130), (256, 64), (512, 3)])
 @pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_FP16X2])
 def test_contraction_kernels_agree_bitwise(bw, nb, prec):
-    """The warp-specialised kernel (tensor-map TMA and cp.async data paths) and the per-chunk-staged
-    kernel do the same arithmetic per work item: forward and inverse outputs are identical bit for bit."""
+    """The warp-specialised kernel's two data paths (tensor-map TMA and per-thread cp.async) do the
+    same arithmetic per work item: forward and inverse outputs are identical bit for bit."""
     torch = _torch()
     lib = api.load()
     rng = np.random.default_rng(bw * 7 + nb)
@@ -234,7 +234,7 @@ def test_contraction_kernels_agree_bitwise(bw, nb, prec):
     c32r, c32i = torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda()
     outs = []
     try:
-        for which in (0, 1, 2):
+        for which in (1, 2):
             assert lib.s2g_set_contraction_kernel(which) == 0
             g = torch.full((nb, 4 * bw * bw), float("nan"), dtype=torch.float32, device="cuda")
             plan.inv_fst_real_f32(c32r, c32i, g, nb, prec)
