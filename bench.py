@@ -412,6 +412,7 @@ def main():
     big1024 = large_bw1024_bench(api, torch, stream, args.seed) if args.group else None
     cplx = complex_bench(api, torch, stream, args.seed) if args.group else None
     odd = odd_bw_bench(api, torch, stream, args.seed) if args.group else None
+    np2 = nonpow2_split_bench(api, torch, stream, args.seed) if args.group else None
     clk = clocks.stop()
 
     # ---- CPU baseline (rank 0): bounded sample of the same workload on all host cores
@@ -453,6 +454,7 @@ def main():
             "large_bw1024_x16": big1024,
             "complex": cplx,
             "odd_bw255_fp64": odd,
+            "split_bw192_x256": np2,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -520,6 +522,38 @@ def odd_bw_bench(api, torch, stream, seed):
     err = (torch.hypot(o_r - d_rc, o_i - d_ic).amax(dim=1) / torch.hypot(d_rc, d_ic).amax(dim=1)).max().item()
     return {"workload": "32 real functions at bw 255, (1+l)^-1, plain FP64, fwd+inv", "value": N / (ms / 1e3),
             "unit": "fwd+inv functions/s", "ms_per_step": ms, "roundtrip_err": err}
+
+
+def nonpow2_split_bench(api, torch, stream, seed):
+    """256 real functions at bw 192 (2 bw = 384 = 32 x 12, not a power of two: the warp FFTs' direct
+    12-point register DFT) on the split path, BF16X3 fwd+inv, with the error of the split forward
+    against the FP64 path."""
+    B, N = 192, 256
+    rc, ic = real_field_coeffs(np.random.default_rng(seed + 192), B, 1.0, N)
+    plan = api.Plan(B, B)
+    d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
+    g64 = torch.empty(N, 4 * B * B, dtype=torch.float64, device="cuda")
+    plan.inv_fst(d_rc, d_ic, g64, None, N, api.REAL, stream)
+    f_r, f_i = torch.empty_like(d_rc), torch.empty_like(d_ic)
+    plan.fst(g64, None, f_r, f_i, N, api.REAL, stream)
+    g32 = g64.float()
+    c_r, c_i = d_rc.float(), d_ic.float()
+    s_r = torch.empty(N, B * B, dtype=torch.float32, device="cuda")
+    s_i = torch.empty_like(s_r)
+    g_out = torch.empty_like(g32)
+
+    def step():
+        plan.inv_fst_real_f32(c_r, c_i, g_out, N, api.PREC_BF16X3, stream)
+        plan.fst_real_f32(g32, s_r, s_i, N, api.PREC_BF16X3, stream)
+
+    ms = _time(torch, stream, step, 20)
+    torch.cuda.synchronize()
+    plan.sync_status()
+    mag = torch.hypot(f_r, f_i).amax(dim=1)
+    err = (torch.hypot(s_r.double() - f_r, s_i.double() - f_i).amax(dim=1) / mag).max().item()
+    e_inv = ((g_out.double() - g64).abs().amax(dim=1) / g64.abs().amax(dim=1)).max().item()
+    return {"workload": "256 real functions at bw 192, (1+l)^-1, split BF16X3, fwd+inv", "value": N / (ms / 1e3),
+            "unit": "fwd+inv functions/s", "ms_per_step": ms, "coeff_err_vs_fp64": err, "grid_err_vs_fp64": e_inv}
 
 
 def complex_bench(api, torch, stream, seed):

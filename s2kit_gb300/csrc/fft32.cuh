@@ -1,10 +1,12 @@
-// fft32.cuh -- warp-level FP32 complex FFT of length n = 32 R (R = 1 .. 32), used by the
-// split-precision pipeline for the longitude DFTs and the latitude DCTs.
+// fft32.cuh -- warp-level FP32 complex FFT of length n = 32 R (R = 1 .. 32, and R = 3 .. 15 that are
+// not powers of two), used by the split-precision pipeline for the longitude DFTs and the
+// latitude DCTs.
 //
 // Decomposition n = R x 32 with input index q = lane + 32 i (lane < 32, i < R):
 //   X[k1 + R k2] = sum_lane w32^(lane k2) [ w_n^(lane k1) sum_i x[lane + 32 i] w_R^(i k1) ]
 //   (a) R-point DFT over the registers of each lane (radix-2, fully unrolled; its twiddles
-//       are compile-time constants, bit reversal is register renaming)
+//       are compile-time constants, bit reversal is register renaming; for R not a power of
+//       two a direct R-point DFT with compile-time twiddles)
 //   (b) twiddle by w_n^(lane k1)
 //   (c) 32-point decimation-in-frequency DFT across the lanes with __shfl_xor_sync
 // On return register k1 of lane l holds X[k1 + R * brev5(l)].
@@ -122,9 +124,44 @@ struct RegStages<R, 2 * R> {
     __device__ __forceinline__ static void run(float2*, float) {}
 };
 
+// Direct R-point DFT in registers for R that is not a power of two: y[K] = sum_J x[J] w_R^(J K),
+// w_R = exp(sign 2 pi i / R), with compile-time twiddles (angles 2 pi e / R evaluated as
+// 2 pi (4 e) / (4 R), whose quadrant reduction keeps the series on [0, pi/4]).
+template <int R, int K, int J>
+struct DftTerm {
+    __device__ __forceinline__ static void run(const float2* x, float2& acc, float sign) {
+        constexpr int e = (J * K) % R;
+        constexpr float c = ct::cosf_(4 * e, 4 * R);
+        constexpr float s = ct::sinf_(4 * e, 4 * R);
+        const float ss = sign * s;
+        acc.x += x[J].x * c - x[J].y * ss;
+        acc.y += x[J].x * ss + x[J].y * c;
+        DftTerm<R, K, J + 1>::run(x, acc, sign);
+    }
+};
+template <int R, int K>
+struct DftTerm<R, K, R> {
+    __device__ __forceinline__ static void run(const float2*, float2&, float) {}
+};
+template <int R, int K>
+struct DftOut {
+    __device__ __forceinline__ static void run(const float2* x, float2* y, float sign) {
+        float2 acc = x[0];
+        DftTerm<R, K, 1>::run(x, acc, sign);
+        y[K] = acc;
+        DftOut<R, K + 1>::run(x, y, sign);
+    }
+};
+template <int R>
+struct DftOut<R, R> {
+    __device__ __forceinline__ static void run(const float2*, float2*, float) {}
+};
+
 template <int R>
 struct WarpFFT {
+    static constexpr bool kPow2 = (R & (R - 1)) == 0;
     __host__ __device__ static constexpr int brev(int i) {
+        if (!kPow2) return i;
         int r = 0;
         for (int b = 1, c = R >> 1; b < R; b <<= 1, c >>= 1)
             if (i & b) r |= c;
@@ -136,11 +173,15 @@ struct WarpFFT {
                                float sign) {
         constexpr int n = 32 * R;
         const int lane = threadIdx.x & 31;
-        // (a) in-register DIT over i
+        // (a) in-register DIT over i (radix 2; a direct DFT when R is not a power of two)
         float2 u[R];
+        if constexpr (kPow2) {
 #pragma unroll
-        for (int i = 0; i < R; ++i) u[brev(i)] = v[i];
-        RegStages<R, 2>::run(u, sign);
+            for (int i = 0; i < R; ++i) u[brev(i)] = v[i];
+            RegStages<R, 2>::run(u, sign);
+        } else {
+            DftOut<R, 0>::run(v, u, sign);
+        }
         // (b) w_n^(lane k1)
 #pragma unroll
         for (int k1 = 1; k1 < R; ++k1) {

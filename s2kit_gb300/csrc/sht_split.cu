@@ -118,7 +118,7 @@ __host__ __device__ __forceinline__ Geo geo(bool fwd, int B, int m) {
         g.KX = nr0;
         const int nbn = B < kNBN ? B : kNBN;
         g.NP = nv ? nbn : round16(B / 2);
-        g.nblk = nv ? B / nbn : 1;
+        g.nblk = nv ? (B + nbn - 1) / nbn : 1;  // the last block is partial when kNBN does not divide B
     }
     g.nch = (g.KX + kKC - 1) / kKC;
     return g;
@@ -323,12 +323,23 @@ static int pack_blobs(Tables* t, Split* s, bool f16, cudaStream_t st) {
     return r;
 }
 
+// Bandwidths of the split path: powers of two 16 .. 1024 (transform lengths 32 R, R a power of
+// two) and the multiples of 16 from 48 to 240 (R = 3 .. 15: the warp FFT's direct register DFT).
+static bool split_bw_ok(int B) {
+    if (B < 16 || B > 1024) return false;
+    if ((B & (B - 1)) == 0) return true;
+    return B % 16 == 0 && B / 16 <= 15;
+}
+
 static int build_split(Tables* t) {
     std::lock_guard<std::mutex> lk(g_split_mu);
     if (t->split) return S2G_OK;
     const int B = t->bw, S = 2 * B;
-    if ((B & (B - 1)) || B < 16 || B > 1024)
-        return fail(S2G_ERR_UNSUPPORTED, "split-precision path needs a power-of-two bw in [16, 1024] (got %d)", B);
+    if (!split_bw_ok(B))
+        return fail(S2G_ERR_UNSUPPORTED,
+                    "split-precision path needs a power-of-two bw in [16, 1024] or a multiple of 16 in [48, 240] "
+                    "(got %d)",
+                    B);
     if (t->cutoff != B) return fail(S2G_ERR_UNSUPPORTED, "split-precision path is seminaive at every order (cutoff == bw)");
     Split* s = new Split();
     s->B = B;
@@ -403,7 +414,7 @@ __device__ __forceinline__ void load_tw(float2* tw, float2* twb, float2* twD, co
                                         int S) {
     for (int k = threadIdx.x; k < S; k += blockDim.x) {
         tw[padtw(k)] = gS[k];
-        twb[k] = gS[((k & 31) * (k >> 5)) & (S - 1)];
+        twb[k] = gS[((k & 31) * (k >> 5)) % S];
         if (twD) twD[k] = gD[k];
     }
 }
@@ -427,8 +438,12 @@ struct FftShape {
     static constexpr int LAT = 2 * W;
     static constexpr int T = 32 * W;
     // resident CTAs per SM the rows-inverse kernel is compiled for: register budgets of 128
-    // (R = 32), 64 (R = 16), 48 (R = 8) and 32 (R <= 4) per thread
-    static constexpr int kMinCtasInv = R == 64 ? 1 : R == 32 ? 2 : R == 16 ? 4 : R == 8 ? 5 : 8;
+    // (R = 32), 64 (R = 16), 48 (R = 8) and 32 (R <= 4) per thread; lengths that are not powers
+    // of two (R = 3 .. 15, the lane-butterfly form with a direct register DFT) 80 above R = 8,
+    // 64 above R = 4, 48 below
+    static constexpr bool kPow2 = (R & (R - 1)) == 0;
+    static constexpr int kMinCtasInv = kPow2 ? (R == 64 ? 1 : R == 32 ? 2 : R == 16 ? 4 : R == 8 ? 5 : 8)
+                                             : (R > 8 ? 3 : R > 4 ? 4 : 5);
     // the rows-forward kernel: 48 registers at R = 8 (5 CTAs per SM; unbounded it takes 62 and
     // runs 4% slower); 0 leaves the other lengths unbounded
     static constexpr int kMinCtasFwd = R == 8 ? 5 : 0;
@@ -508,7 +523,7 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ grid, fl
     // (k >= B) at wi[2 pad32(k - B)] (the warp's two plane segments), so that the output phase
     // reads each value with one 8-byte load (-1 to -2%).  Otherwise planes wr/wi[pad32(k)] (at
     // R <= 4 the pairs cost registers and occupancy: +14% at R = 4).
-    constexpr bool kPairSpec = R >= 8 && R <= 32;
+    constexpr bool kPairSpec = R == 8 || R == 16 || R == 32;
     if constexpr (R == 64) {
         WarpFFT2048::to_spectrum([&](int j) { return make_float2(ra[j], ra[S + j]); }, tw, twb, twc, wr, wi, -1.f);
     } else {
@@ -541,7 +556,7 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ grid, fl
             const float* zi = spi + (q / 2 + h) * PSA;
             float ar, ai, br, bi;
             if constexpr (!kPairSpec) {
-                const int pmm = pad32((S - m) & (S - 1));
+                const int pmm = pad32((S - m) % S);
                 ar = zr[pm], ai = zi[pm], br = zr[pmm], bi = zi[pmm];
             } else {
                 // Z[m] (m < B) and Z[S - m] (S - m > B, or Z[0] for m = 0)
@@ -681,7 +696,7 @@ __device__ __forceinline__ void dct_fwd_body(float* __restrict__ X, float* __res
         for (int u = 0; u < 4; ++u) {
             const int o = 4 * e + u;                         // o = (k & 1) * B/2 + k/2
             const int k = o < B / 2 ? 2 * o : 2 * (o - B / 2) + 1;
-            const int kk = (S - k) & (S - 1);
+            const int kk = (S - k) % S;
             const float ar = wr[pad32(k)], ai = wi[pad32(k)], br = wr[pad32(kk)], bi = wi[pad32(kk)];
             const float2 cs = twP[u * (B / 4) + e];
             const float c = cs.x, sn = cs.y;
@@ -1192,12 +1207,13 @@ __device__ __forceinline__ void epi_store(const LegClass& K, int m, int t, int n
             for (int j = lane; j < nj; j += 32) dst[j] = src[j] * ((c0 + j + t) == 0 ? sc0 : sc_);
         }
     } else {
+        const int wn = min(w, B - nb * NP - c0);  // latitudes of a partial last block end at B
         for (int r = wid; r < 128; r += nw) {
             const int f = f0 + (r & 63), part = r >> 6;
             if (f >= K.N) continue;
             const float* src = ep + r * ES;
             float* dst = K.F + (((size_t)part * K.N + f) * B + m) * (2 * B) + t * B + nb * NP + c0;
-            for (int i = lane; i < w; i += 32) dst[i] = src[i];
+            for (int i = lane; i < wn; i += 32) dst[i] = src[i];
         }
     }
 }
@@ -2231,8 +2247,9 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     long long items = 0;
     int nbmax = 16;
     // tensor-map TMA path: one class, BF16 terms, contiguous batches, bw >= 64, warp-specialised kernel
+    // (power-of-two bw: the inverse's 32-column output boxes then never reach into the other parity)
     const bool want_tma = g_leg_tma && !f16 && ncls == 1 && !spec[0].cmap &&
-                          spec[0].t->bw >= 64;
+                          spec[0].t->bw >= 64 && (spec[0].t->bw & (spec[0].t->bw - 1)) == 0;
     for (int c = 0; c < ncls; ++c) {
         const LegSpec& q = spec[c];
         S2G_TRY(f16 ? build_split16(q.t) : build_split(q.t));
@@ -2335,8 +2352,20 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
 
 static int fft_kernels(int which, int B, const void* in, void* out, int N, const Split* s, cudaStream_t st,
                        float scale, const int64_t* gmap = nullptr) {
+    if ((2 * B) % 32) return fail(S2G_ERR_UNSUPPORTED, "no warp FFT for bandwidth %d", B);
     switch (2 * B / 32) {
         case 1: return launch_fft_kernels<1>(which, in, out, N, s, st, scale, gmap);
+        case 3: return launch_fft_kernels<3>(which, in, out, N, s, st, scale, gmap);
+        case 5: return launch_fft_kernels<5>(which, in, out, N, s, st, scale, gmap);
+        case 6: return launch_fft_kernels<6>(which, in, out, N, s, st, scale, gmap);
+        case 7: return launch_fft_kernels<7>(which, in, out, N, s, st, scale, gmap);
+        case 9: return launch_fft_kernels<9>(which, in, out, N, s, st, scale, gmap);
+        case 10: return launch_fft_kernels<10>(which, in, out, N, s, st, scale, gmap);
+        case 11: return launch_fft_kernels<11>(which, in, out, N, s, st, scale, gmap);
+        case 12: return launch_fft_kernels<12>(which, in, out, N, s, st, scale, gmap);
+        case 13: return launch_fft_kernels<13>(which, in, out, N, s, st, scale, gmap);
+        case 14: return launch_fft_kernels<14>(which, in, out, N, s, st, scale, gmap);
+        case 15: return launch_fft_kernels<15>(which, in, out, N, s, st, scale, gmap);
         case 2: return launch_fft_kernels<2>(which, in, out, N, s, st, scale, gmap);
         case 4: return launch_fft_kernels<4>(which, in, out, N, s, st, scale, gmap);
         case 8: return launch_fft_kernels<8>(which, in, out, N, s, st, scale, gmap);

@@ -61,7 +61,10 @@ def _nerr(got, ref):
     return (d / ref.abs().amax(dim=1)).max().item()
 
 
-@pytest.mark.parametrize("bw,nb", [(16, 3), (32, 70), (64, 10), (128, 65), (256, 130), (512, 2)])
+@pytest.mark.parametrize("bw,nb", [(16, 3), (32, 70), (64, 10), (128, 65), (256, 130), (512, 2),
+                                   # multiples of 16 that are not powers of two (transform lengths
+                                   # 32 R, R = 3 .. 15; bw 144 and 240 have a partial naive block)
+                                   (48, 5), (80, 70), (112, 3), (144, 65), (192, 33), (208, 2), (240, 4)])
 @pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_BF16X2, api.PREC_FP16X2])
 def test_split_forward_inverse_vs_fp64(bw, nb, prec):
     torch = _torch()
@@ -87,6 +90,30 @@ def test_split_forward_inverse_vs_fp64(bw, nb, prec):
     tol = 5e-6 if (prec == api.PREC_FP16X2 and bw > 256) else TOL[prec]
     assert e_fwd <= tol, e_fwd
     assert e_inv <= tol, e_inv
+
+
+@pytest.mark.parametrize("bw", [96, 192])
+def test_split_non_power_of_two_vs_oracle(oracle, bw):
+    """A bandwidth that is not a power of two (lengths 2 bw = 32 R, R = 6 and 12) on the split
+    path against the oracle directly: forward of the oracle's samples and inverse of the
+    coefficients, BF16X3 tolerance."""
+    torch = _torch()
+    nb = 2
+    rng = np.random.default_rng(bw)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    grids = np.stack([oracle.inv_fst(rc[f], ic[f], bw, api.REAL, bw)[0] for f in range(nb)])
+    plan = api.Plan(bw, bw)
+    s_rc = torch.zeros(nb, bw * bw, dtype=torch.float32, device="cuda")
+    s_ic = torch.zeros_like(s_rc)
+    plan.fst_real_f32(torch.from_numpy(grids).float().cuda(), s_rc, s_ic, nb, api.PREC_BF16X3)
+    s_grid = torch.zeros(nb, 4 * bw * bw, dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda(), s_grid, nb,
+                          api.PREC_BF16X3)
+    plan.sync_status()
+    mag = np.hypot(rc, ic).max(axis=1)
+    e_f = (np.hypot(s_rc.double().cpu().numpy() - rc, s_ic.double().cpu().numpy() - ic).max(axis=1) / mag).max()
+    e_i = (np.abs(s_grid.double().cpu().numpy() - grids).max(axis=1) / np.abs(grids).max(axis=1)).max()
+    assert e_f <= TOL[api.PREC_BF16X3] and e_i <= TOL[api.PREC_BF16X3], (e_f, e_i)
 
 
 def test_split_matches_oracle_and_roundtrip(oracle):
@@ -212,10 +239,11 @@ def test_split_host_api_matches_device_api():
 def test_split_rejects_unsupported():
     import s2kit_gb300 as s2
     torch = _torch()
-    plan = api.Plan(24, 24)  # not a power of two
-    x = torch.zeros(4 * 24 * 24, device="cuda")
-    with pytest.raises(s2.S2GError):
-        plan.fst_real_f32(x, x, x, 1, api.PREC_BF16X3)
+    for bw in (24, 200, 272):  # not a power of two, and not a multiple of 16 in [48, 240]
+        plan = api.Plan(bw, bw)
+        x = torch.zeros(4 * bw * bw, device="cuda")
+        with pytest.raises(s2.S2GError):
+            plan.fst_real_f32(x, x, x, 1, api.PREC_BF16X3)
     plan64 = api.Plan(64, 64)
     with pytest.raises(s2.S2GError):
         plan64.fst_real_f32(x, x, x, 1, 7)  # unknown precision
