@@ -1028,7 +1028,8 @@ struct Leg {
     uint32_t a_chunk_bytes;   // TMA bytes of one A chunk
     int pair;                 // forward: items come in parity pairs; the odd item writes both (see k_leg_ws)
     int stall;                // test hook: the scheduler publishes no work (every other wait runs out)
-    uint32_t stash_off;       // forward pairs: shared-memory offset of the even parity's results
+    uint32_t stash_off;       // forward pairs: shared-memory offset of the even parity's results (group 0)
+    uint32_t epi_stride;      // bytes between the two epilogue groups' staging (and stash) areas
     int stash_stride;         // ... and their row stride in floats (odd)
     CUtensorMap tmA0, tmA1;   // forward: C, folded X; inverse: rc, ic
     CUtensorMap tmO;          // inverse: Fc
@@ -1258,8 +1259,11 @@ __device__ __forceinline__ void issue_table(uint8_t* sb, const uint8_t* blob, in
 //                and table producer (bulk copies into an nbs-stage ring);
 //   warp 1     : MMA issuer (one thread; two accumulator pairs in TMEM when they fit, so the
 //                epilogue of item k overlaps the MMAs of item k+1);
-//   warps 4-7  : epilogue (warp 4+q reads TMEM lanes 32q..32q+31 = accumulator rows, stages
-//                128-column blocks in shared memory, writes them coalesced);
+//   warps 4-7 and 16-19: two epilogue groups taking alternate work items (alternate parity pairs
+//                in pair mode); warp 4+q (16+q) reads TMEM lanes 32q..32q+31 = accumulator rows,
+//                stages column blocks in its group's shared memory, writes them coalesced.  One
+//                group was the busiest role of the kernel (82-91% busy against 40-58% for the MMA
+//                thread and the A producers, measured with per-role clock counters);
 //   warps 8-15 : A producers (FP32 loads one chunk ahead, split, store into a kNAS-stage ring);
 //   warp 2     : on the tensor-map path, A loader: one TMA per chunk into the FP32 staging ring,
 //                paced by that ring alone, so the A operand (from HBM) runs up to nstg chunks
@@ -1268,7 +1272,7 @@ __device__ __forceinline__ void issue_table(uint8_t* sb, const uint8_t* blob, in
 // Every mbarrier wait is bounded; on expiry the role records the abort and leaves its loop,
 // the table producer waits (bounded) for its copies in flight, the MMA thread for its MMAs,
 // and the CTA frees TMEM and returns.
-static constexpr int kWsThreads = 512;
+static constexpr int kWsThreads = 640;
 static constexpr int kNI = 4;          // item ring entries
 static constexpr int kNAS = 2;         // A stages
 static constexpr int kMaxNBS = 8;      // table stages (upper bound)
@@ -1281,6 +1285,21 @@ static constexpr uint32_t kStgBytes = kAProd * kTasks * 8 * sizeof(float);  // o
 struct WsItem {
     int ci, m, t, sub, nb, f0;
 };
+
+// The TMEM accumulator pair of item k and how many items used that pair before it.  A pair's
+// mbarriers are waited on by parity, so every use of one pair must go to the same epilogue group
+// (a group waiting for use u while use u-1 is still open would see use u-2's parity and pass):
+// with two pairs and two groups, group g owns pair g; in forward pair mode a parity pair (k, k+1)
+// shares one accumulator pair, since the even item frees it at once after stashing its results.
+// With one pair (wide blocks) there is one epilogue group.
+struct AccUse {
+    int buf, use;
+};
+__device__ __forceinline__ AccUse acc_use(int k, int nacc, bool pair) {
+    if (nacc == 1) return {0, k};
+    if (pair) return {(k >> 1) & 1, ((k >> 2) << 1) | (k & 1)};
+    return {k & 1, k >> 1};
+}
 
 // The K chunks an item multiplies, [c0, c1), and per chunk the N rows [r0, r0 + n) its MMAs cover.
 // The seminaive table of order m is zero where the cosine frequency index j exceeds m/2 + i, i the
@@ -1710,7 +1729,21 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 }
                 items[slot] = e;
                 tc::mbar_arrive(&item_full[slot]);
-                if (e.ci < 0) break;
+                if (e.ci < 0) {
+                    // each epilogue group stops at the first end marker it sees: publish the marker
+                    // for the next three items too, so the other group meets one whichever items
+                    // (or, in pair mode, parity pairs) it takes
+                    for (int x = 1; x <= 3 && !s_abort; ++x) {
+                        const int sl = (k + x) % kNI;
+                        if (!tc::mbar_wait(&item_empty[sl], (((k + x) / kNI) & 1) ^ 1)) {
+                            s_abort = 1;
+                            break;
+                        }
+                        items[sl] = e;
+                        tc::mbar_arrive(&item_full[sl]);
+                    }
+                    break;
+                }
                 const LegClass& K = p.cls[e.ci];
                 const Geo g = geo(FWD, K.B, e.m);
                 const int n0 = e.sub * K.NB, rows = min(K.NB, g.NP - n0);
@@ -1784,8 +1817,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 const int n0 = e.sub * K.NB, rows = min(K.NB, g.NP - n0);
                 const Span sp = item_span(FWD, g.nch, e.m, n0, rows);
                 const uint32_t bpart = (uint32_t)rows * kKC * 2;
-                const int buf = k % nacc;
-                if (!tc::mbar_wait(&acc_empty[buf], ((k / nacc) & 1) ^ 1)) {
+                const AccUse au = acc_use(k, nacc, FWD && p.pair);
+                const int buf = au.buf;
+                if (!tc::mbar_wait(&acc_empty[buf], (au.use & 1) ^ 1)) {
                     s_abort = 1;
                     break;
                 }
@@ -1837,23 +1871,29 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             tc::mma_commit(&fin);
             tc::mbar_wait(&fin, 0);
         }
-    } else if (warp >= 4 && warp < 8) {
-        // ---------------- epilogue ----------------
-        const int et = threadIdx.x - 128;  // accumulator row = TMEM lane
-        float* ep = reinterpret_cast<float*>(smem + epi_off);
+    } else if ((warp >= 4 && warp < 8) || (warp >= 16 && nacc == 2)) {
+        // ---------------- epilogue (two groups with two accumulator pairs, else one) ----------------
+        const int grp = warp >= 16 ? 1 : 0;
+        const int ebar = 1 + grp;                        // the group's named barrier
+        const int et = ((warp & 3) << 5) | lane;         // accumulator row = TMEM lane
+        float* ep = reinterpret_cast<float*>(smem + epi_off + grp * p.epi_stride);
         constexpr int ES = kEpiCols + 1;   // odd row stride
         uint32_t eblk = 0;                 // TMA-store blocks written (staging buffer eblk & 1)
-        for (int k = 0;; ++k) {
+        for (int i = 0;; ++i) {
+            // this group's i-th item: every item with one group; else alternate items, or
+            // alternate parity pairs in pair mode (the items of the group's accumulator pair)
+            const int k = nacc == 1 ? i : (FWD && p.pair) ? 4 * (i >> 1) + 2 * grp + (i & 1) : 2 * i + grp;
             const int slot = k % kNI;
-            const int buf = k % nacc;
+            const AccUse au = acc_use(k, nacc, FWD && p.pair);
+            const int buf = au.buf;
             bool ok = tc::mbar_wait(&item_full[slot], (k / kNI) & 1);
             WsItem e = items[slot];
             if (ok && e.ci >= 0) {
-                ok = tc::mbar_wait(&acc_full[buf], (k / nacc) & 1);
+                ok = tc::mbar_wait(&acc_full[buf], au.use & 1);
                 if (ok && F16) ok = tc::mbar_wait(&sc_full[slot], (k / kNI) & 1);
             }
-            // the 128 epilogue threads take every decision below together (they share named barriers)
-            if (!tc::named_bar_and(1, kEpi, ok && !s_abort)) {
+            // the group's 128 threads take every decision below together (they share named barriers)
+            if (!tc::named_bar_and(ebar, kEpi, ok && !s_abort)) {
                 s_abort = 1;
                 break;
             }
@@ -1871,7 +1911,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             if (FWD && p.pair) {
                 // parity pairs: the even item (k even) parks its results in the stash and frees its
                 // accumulator at once; the odd item interleaves both parities in l and stores whole runs
-                float* stash = reinterpret_cast<float*>(smem + p.stash_off);
+                float* stash = reinterpret_cast<float*>(smem + p.stash_off + grp * p.epi_stride);
                 const int SST = p.stash_stride;
                 if (t != (k & 1)) {  // not a pair in order (never expected): abort, reported as a device error
                     s_abort = 1;
@@ -1905,9 +1945,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                         ep[et * PS + 2 * q] = stash[et * SST + cb0 + q];
                         ep[et * PS + 2 * q + 1] = v[q] * rs;
                     }
-                    tc::named_bar_sync(1, kEpi);
-                    epi_store_pair(K, m, e.f0, n0 + cb0, ep, PS, warp - 4, 4, lane);
-                    tc::named_bar_sync(1, kEpi);
+                    tc::named_bar_sync(ebar, kEpi);
+                    epi_store_pair(K, m, e.f0, n0 + cb0, ep, PS, warp & 3, 4, lane);
+                    tc::named_bar_sync(ebar, kEpi);
                 }
                 tc::mbar_arrive(&item_empty[slot]);
                 continue;
@@ -1918,7 +1958,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 for (int cb0 = 0; cb0 < rows; cb0 += 32, ++eblk) {
                     uint8_t* eb = reinterpret_cast<uint8_t*>(ep) + (eblk & 1) * 16384;
                     if (et == 0) tc::bulk_wait_read1();  // the store that last read this buffer is done
-                    tc::named_bar_sync(1, kEpi);
+                    tc::named_bar_sync(ebar, kEpi);
                     float v[32];
                     ld_sum(trow + cb0, corr, p.nprod > 1, v);
                     ld_sum(trow + cb0 + 16, corr, p.nprod > 1, v + 16);
@@ -1935,7 +1975,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                         *reinterpret_cast<float4*>(eb + et * 128 + ((u ^ (et & 7)) << 4)) = w4;
                     }
                     tc::fence_proxy_async_smem();
-                    tc::named_bar_sync(1, kEpi);
+                    tc::named_bar_sync(ebar, kEpi);
                     if (et == 0) {
                         tc::tma_store_4d(&p.tmO, t * (B / 2) + j0, m, e.f0, 0, eb);
                         tc::bulk_commit();
@@ -1946,7 +1986,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             }
             if (!FWD && p.tma) {  // the plain path below reuses the staging: no store may still read it
                 if (et == 0) tc::bulk_wait_read0();
-                tc::named_bar_sync(1, kEpi);
+                tc::named_bar_sync(ebar, kEpi);
             }
             for (int cb0 = 0; cb0 < rows; cb0 += kEpiCols) {
                 const int w = min(kEpiCols, rows - cb0);
@@ -1960,22 +2000,22 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                     tc::tc_fence_before();
                     tc::mbar_arrive(&acc_empty[buf]);
                 }
-                tc::named_bar_sync(1, kEpi);
-                epi_store<FWD>(K, m, t, e.nb, g.NP, e.f0, n0 + cb0, w, ep, ES, warp - 4, 4, lane);
-                tc::named_bar_sync(1, kEpi);
+                tc::named_bar_sync(ebar, kEpi);
+                epi_store<FWD>(K, m, t, e.nb, g.NP, e.f0, n0 + cb0, w, ep, ES, warp & 3, 4, lane);
+                tc::named_bar_sync(ebar, kEpi);
             }
             tc::mbar_arrive(&item_empty[slot]);
         }
         if (et == 0) tc::bulk_wait_all();  // TMA stores complete before the CTA leaves
-    } else if (warp >= 8 && !F16 && p.tma) {
+    } else if (warp >= 8 && warp < 16 && !F16 && p.tma) {
         // ---------------- A producers (BF16 terms): staging filled by tensor-map TMA ----------------
         produce_a_tma<FWD>(p, smem, smem + stg_off, stg_stride, nstg, items, item_full, item_empty, stg_full,
                            stg_empty, a_full, a_empty, &s_abort, threadIdx.x - 256);
-    } else if (warp >= 8 && !F16) {
+    } else if (warp >= 8 && warp < 16 && !F16) {
         // ---------------- A producers (BF16 terms): asynchronous staging ----------------
         produce_a_async<FWD>(p, smem, reinterpret_cast<float4*>(smem + stg_off), nstg, items, item_full, item_empty,
                              a_full, a_empty, &s_abort, threadIdx.x - 256);
-    } else if (warp >= 8) {
+    } else if (warp >= 8 && warp < 16) {
         // ---------------- A producers (FP16 terms): row scales first, loads in registers ----------------
         const int tid = threadIdx.x - 256;
         uint32_t ac = 0;
@@ -2101,14 +2141,17 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     // cp.async path, per-thread slots.  As many stages as leave room for two table stages.
     const size_t stg_stride = p.tma ? ((size_t)p.a_chunk_bytes + 1023) & ~(size_t)1023 : kStgBytes;
     // forward parity pairs (whole sectors in the coefficient stores): the even parity's results
-    // wait in a stash of 128 rows x (nbmax + 1) floats and the interleave tile is 128 x 33; taken
-    // when that still leaves two table stages and four A staging stages (at bw 256 the stash would
-    // cut the staging to two, and the shallower A prefetch costs more than the whole sectors gain)
+    // wait in a stash of 128 rows x (nbmax + 1) floats and the interleave tile is 128 x 33, one of
+    // each per epilogue group; taken when that still leaves two table stages and four A staging
+    // stages (at bw 256 the stash would cut the staging to two, and the shallower A prefetch costs
+    // more than the whole sectors gain)
+    const int ngrp = nacc;  // epilogue groups: one per accumulator pair (see acc_use)
     p.pair = 0;
     if (fwd && nbmax <= 128) {
         const size_t stash = ((size_t)128 * (nbmax + 1) * sizeof(float) + 1023) & ~(size_t)1023;
         const size_t tile = ((size_t)128 * 33 * sizeof(float) + 1023) & ~(size_t)1023;
-        const long long need = (long long)(a_bytes + (f16 ? 0 : 4 * stg_stride) + 2 * b_stage + tile + stash);
+        const long long need =
+            (long long)(a_bytes + (f16 ? 0 : 4 * stg_stride) + 2 * b_stage + ngrp * (tile + stash));
         if (need <= budget) {
             p.pair = 1;
             p.stash_stride = nbmax + 1;
@@ -2119,7 +2162,7 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     const int nstg_min = p.tma ? 1 : 2;
     long long nbs_fit = 0;
     for (;;) {
-        nbs_fit = (budget - (long long)a_bytes - (long long)nstg * (long long)stg_stride - (long long)epi) /
+        nbs_fit = (budget - (long long)a_bytes - (long long)nstg * (long long)stg_stride - ngrp * (long long)epi) /
                   (long long)b_stage;
         if (nbs_fit >= 2 || nstg <= nstg_min || f16) break;
         --nstg;
@@ -2127,7 +2170,8 @@ static int launch_leg_ws(bool fwd, bool f16, Leg& p, int nbmax, long long items,
     const int nbs = (int)std::min<long long>(table_stages > 0 ? std::min(table_stages, kMaxNBS) : kMaxNBS, nbs_fit);
     if (nbs < 2) return fail(S2G_ERR_UNSUPPORTED, "warp-specialised contraction does not fit in shared memory");
     const size_t stg_bytes = (size_t)nstg * stg_stride;
-    const size_t smem = 1024 + a_bytes + stg_bytes + (size_t)nbs * b_stage + epi;
+    const size_t smem = 1024 + a_bytes + stg_bytes + (size_t)nbs * b_stage + ngrp * epi;
+    p.epi_stride = (uint32_t)epi;
     S2G_TRY(set_smem(fn, smem));
     const int grid = (int)std::min<long long>(items, nsm);
     S2G_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
