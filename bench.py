@@ -412,7 +412,8 @@ def main():
     big1024 = large_bw1024_bench(api, torch, stream, args.seed) if args.group else None
     cplx = complex_bench(api, torch, stream, args.seed) if args.group else None
     odd = odd_bw_bench(api, torch, stream, args.seed) if args.group else None
-    np2 = nonpow2_split_bench(api, torch, stream, args.seed) if args.group else None
+    np2 = nonpow2_split_bench(api, torch, stream, args.seed, 192) if args.group else None
+    odd_split = nonpow2_split_bench(api, torch, stream, args.seed, 255) if args.group else None
     clk = clocks.stop()
 
     # ---- CPU baseline (rank 0): bounded sample of the same workload on all host cores
@@ -455,6 +456,7 @@ def main():
             "complex": cplx,
             "odd_bw255_fp64": odd,
             "split_bw192_x256": np2,
+            "split_bw255_x256": odd_split,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -524,12 +526,13 @@ def odd_bw_bench(api, torch, stream, seed):
             "unit": "fwd+inv functions/s", "ms_per_step": ms, "roundtrip_err": err}
 
 
-def nonpow2_split_bench(api, torch, stream, seed):
-    """256 real functions at bw 192 (2 bw = 384 = 32 x 12, not a power of two: the warp FFTs' direct
-    12-point register DFT) on the split path, BF16X3 fwd+inv, with the error of the split forward
-    against the FP64 path."""
-    B, N = 192, 256
-    rc, ic = real_field_coeffs(np.random.default_rng(seed + 192), B, 1.0, N)
+def nonpow2_split_bench(api, torch, stream, seed, B):
+    """256 real functions at a bandwidth that is not a power of two on the split path, BF16X3
+    fwd+inv, with the errors of the split forward and inverse against the FP64 path.  bw 192:
+    2 bw = 384 = 32 x 12, the warp FFTs' direct 12-point register DFT; bw 255: 2 bw = 510, every
+    length-510 DFT a chirp-z transform over warp FFTs of length 1024."""
+    N = 256
+    rc, ic = real_field_coeffs(np.random.default_rng(seed + B), B, 1.0, N)
     plan = api.Plan(B, B)
     d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
     g64 = torch.empty(N, 4 * B * B, dtype=torch.float64, device="cuda")
@@ -552,7 +555,7 @@ def nonpow2_split_bench(api, torch, stream, seed):
     mag = torch.hypot(f_r, f_i).amax(dim=1)
     err = (torch.hypot(s_r.double() - f_r, s_i.double() - f_i).amax(dim=1) / mag).max().item()
     e_inv = ((g_out.double() - g64).abs().amax(dim=1) / g64.abs().amax(dim=1)).max().item()
-    return {"workload": "256 real functions at bw 192, (1+l)^-1, split BF16X3, fwd+inv", "value": N / (ms / 1e3),
+    return {"workload": f"256 real functions at bw {B}, (1+l)^-1, split BF16X3, fwd+inv", "value": N / (ms / 1e3),
             "unit": "fwd+inv functions/s", "ms_per_step": ms, "coeff_err_vs_fp64": err, "grid_err_vs_fp64": e_inv}
 
 

@@ -207,8 +207,9 @@ int s2g_conv(s2g_plan plan, const double* rdata, const double* idata, const doub
              const double* ifilter, double* rres, double* ires, int batch, void* stream);
 
 /* Real-field batched transforms with FP32 samples/coefficients and a selectable
- * precision for the Legendre contraction (s2g_precision); power-of-two bw in [16, 1024],
- * plan cutoff == bw.  grid: batch*(2bw)^2 floats;
+ * precision for the Legendre contraction (s2g_precision); any bw in [16, 256] and the powers
+ * of two up to 1024 (lengths 2bw that no warp FFT takes, odd bw among them, run as chirp-z
+ * transforms), plan cutoff == bw.  grid: batch*(2bw)^2 floats;
  * rcoeffs/icoeffs: batch*bw*bw floats in the reference layout, negative orders filled by
  * f(l,-m) = (-1)^m conj f(l,m) on output and ignored on input. */
 int s2g_fst_real_f32(s2g_plan plan, const float* grid, float* rcoeffs, float* icoeffs, int batch, int precision,
@@ -237,7 +238,7 @@ int s2g_inv_fst_complex_f32(s2g_plan plan, const float* rcoeffs, const float* ic
  * samples to FP32, and that rounding noise lies outside the band the residual can see, so the
  * pointwise sample error stays at the FP32 level (about 1e-7).  Both cost one FP64 transform
  * (the residual) plus two split transforms.  Layouts as
- * s2g_fst_real_f32 (the inverse reads the non-negative orders); power-of-two bw in [16, 1024],
+ * s2g_fst_real_f32 (the inverse reads the non-negative orders); bandwidths as s2g_fst_real_f32,
  * plan cutoff == bw.  The plan grows its own scratch. */
 int s2g_fst_refined(s2g_plan plan, const double* grid, double* rcoeffs, double* icoeffs, int batch, int precision,
                     void* stream);

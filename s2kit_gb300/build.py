@@ -21,7 +21,8 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "libs2kit_gb300.so")
 BUILD_DIR = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "tables.cu", "sht_fp64.cu", "sht_split.cu", "group.cu", "refine.cu", "noalloc.cu"]
+SOURCES = ["capi.cu", "tables.cu", "sht_fp64.cu", "sht_split.cu", "czt_split.cu", "group.cu", "refine.cu",
+           "noalloc.cu"]
 CLI_SRC = os.path.join(PKG, "cli", "s2kit_drivers.c")
 BIN_DIR = os.path.join(PKG, "bin")
 CLI_NAMES = ["test_s2_semi_memo_fwd", "test_s2_semi_memo_inv", "test_s2_semi_memo", "test_s2_semi_fly",

@@ -141,7 +141,43 @@ int inv_dlt_naive_f64(const double* coeffs, int bw, int m, double* result, const
                       cudaStream_t st);
 int twiddles_device(int n, double2* d_tw_full, double2* d_tw_quarter, cudaStream_t st);
 
-// ---- split-precision pipeline (sht_split.cu) ----
+// ---- split-precision pipeline (sht_split.cu, czt_split.cu) ----
+// Orders the split path computes with the naive transform: odd m below 32.  For these the cosine
+// series of G = P/sin(theta) has large coefficients, and FP32 rounding of the DCT output is
+// amplified by them (the reference's seminaive/naive hybrid, FST_semi_memo.c:96-120, makes the
+// same trade at the other end of the order range).
+constexpr int kSplitNaiveOddBelow = 32;
+__host__ __device__ __forceinline__ bool split_naive_order(int m) { return (m & 1) && m < kSplitNaiveOddBelow; }
+// Layout of the split path's intermediate arrays at bandwidth bw, per plane (re, im), function
+// and order m < bw: X and F rows of SX floats (latitudes theta < 2bw; a naive order's folded
+// halves at t BN, t = 0, 1), C and Fc rows of 2 BH floats (cosine frequency k = 2j + t at t BH + j).
+// bw itself (BH = bw/2, BN = bw, SX = 2bw) where the warp FFTs take length 2bw; at the chirp-z
+// bandwidths BN and BH are rounded up to multiples of 8, the padding held at zero.
+struct SplitLayout {
+    int BH, BN, SX;
+};
+SplitLayout split_layout(int bw);
+// True where the split path's length-2bw DFTs run as chirp-z transforms (czt_split.cu): bw in
+// [17, 256] and 2bw not a warp-FFT length.
+bool split_czt(int bw);
+// Length M of the chirp-z convolution at bandwidth bw: the power of two >= 4 bw - 1 (at least 128).
+int czt_len(int bw);
+// Device tables of one chirp-z bandwidth (the first three from czt_build_tables, the rest the
+// split path's FP32 weights, sin(theta) and DCT twiddles).
+struct CztTabs {
+    int B, M;
+    const float2* h;     // exp(-i pi (n^2 mod 2S) / S), n < S = 2B
+    const float2* K;     // DFT_M of b_j = conj(h_|j|) (|j| < S, j mod M), divided by M
+    const float2* twM;   // exp(2 pi i k / M), k < M
+    const float* w32;    // quadrature weights, 2S (even orders, then odd)
+    const float* sin32;  // sin(theta_j), S
+    const float2* twD;   // (cos, sin)(pi k / 2S), k < S
+};
+int czt_build_tables(int bw, float2** d_h, float2** d_K, float2** d_tw);
+// One FFT stage (which: 0 rows forward, 1 weighted DCT-II, 2 DCT-III, 3 rows inverse) of N
+// functions at a chirp-z bandwidth; in/out, scale and gmap as the warp-FFT stages.
+int czt_stage(int which, const CztTabs& g, const void* in, void* out, int N, float scale, const int64_t* gmap,
+              cudaStream_t st);
 size_t split_work_bytes(int bw, int batch);
 int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int precision, void* work,
               cudaStream_t st);
@@ -170,7 +206,7 @@ int split_stage_group(int which, const StageSpec* spec, int ncls, int dct_ctas_p
 int split_device_status(Tables* t, int clear);
 
 // One bandwidth class of a (grouped) tensor-core contraction launch.  Intermediate arrays are
-// class-contiguous: X/F [2][N][B][2B], C/Fc [2][N][B][B] floats.
+// class-contiguous: X/F [2][N][B][SX], C/Fc [2][N][B][2 BH] floats (split_layout(B)).
 struct LegSpec {
     Tables* t;
     int N;                    // functions of this class

@@ -56,6 +56,11 @@ struct Split {
     int64_t* fwd16_off = nullptr;
     int64_t* inv16_off = nullptr;
     double tab16 = 0.0;
+    // chirp-z bandwidths (split_czt): chirp, kernel spectrum and length-M twiddles; czM = 0 otherwise
+    int czM = 0;
+    float2* czh = nullptr;
+    float2* czK = nullptr;
+    float2* cztw = nullptr;
     // per (direction, tile N extent NB): the work items of one 64-function tile, in order, as
     // (order m, index j within the order) -- item decoding is one load
     std::vector<std::pair<int, int2*>> itab[2];
@@ -80,6 +85,9 @@ void free_split(Tables* t) {
     cudaFree(s->inv16);
     cudaFree(s->fwd16_off);
     cudaFree(s->inv16_off);
+    cudaFree(s->czh);
+    cudaFree(s->czK);
+    cudaFree(s->cztw);
     for (auto& v : s->itab)
         for (auto& e : v) cudaFree(e.second);
     cudaFree(s->err);
@@ -90,12 +98,9 @@ void free_split(Tables* t) {
 __host__ __device__ __forceinline__ int round16(int x) { return (x + 15) & ~15; }
 __host__ __device__ __forceinline__ int nr_par(int B, int m, int t) { return (B - m - t + 1) / 2; }
 
-// Orders computed with the naive transform in the split path: odd m below 32.  For these the
-// cosine series of G = P/sin(theta) has large coefficients, and FP32 rounding of the DCT
-// output is amplified by them (the reference's seminaive/naive hybrid, FST_semi_memo.c:96-120,
-// makes the same trade at the other end of the order range).
-static constexpr int kNaiveOddBelow = 32;
-__host__ __device__ __forceinline__ bool naive_order(int m) { return (m & 1) && m < kNaiveOddBelow; }
+// Orders computed with the naive transform in the split path (split_naive_order, s2g_internal.h).
+static constexpr int kNaiveOddBelow = kSplitNaiveOddBelow;
+__host__ __device__ __forceinline__ bool naive_order(int m) { return split_naive_order(m); }
 
 static constexpr int kKC = 32;   // K columns per pipeline chunk (two K=16 MMA steps)
 static constexpr int kNBN = 128; // latitude block of the naive inverse (N per CTA)
@@ -110,15 +115,17 @@ __host__ __device__ __forceinline__ Geo geo(bool fwd, int B, int m) {
     Geo g;
     const bool nv = naive_order(m);
     const int nr0 = nr_par(B, m, 0);
+    // (B + 1) / 2: the cosine frequencies k = 2j + t < B of parity 0 (at odd B parity 1 has one fewer)
     if (fwd) {
         g.NP = round16(nr0);
-        g.KX = nv ? B : B / 2;
+        g.KX = nv ? B : (B + 1) / 2;
         g.nblk = 1;
     } else {
         g.KX = nr0;
-        const int nbn = B < kNBN ? B : kNBN;
-        g.NP = nv ? nbn : round16(B / 2);
-        g.nblk = nv ? (B + nbn - 1) / nbn : 1;  // the last block is partial when kNBN does not divide B
+        // latitude blocks of the naive orders: the MMA's N must be a multiple of 16
+        const int nbn = B < kNBN ? round16(B) : kNBN;
+        g.NP = nv ? nbn : round16((B + 1) / 2);
+        g.nblk = nv ? (B + nbn - 1) / nbn : 1;  // the last block is partial when B is not a multiple of it
     }
     g.nch = (g.KX + kKC - 1) / kKC;
     return g;
@@ -324,11 +331,12 @@ static int pack_blobs(Tables* t, Split* s, bool f16, cudaStream_t st) {
 }
 
 // Bandwidths of the split path: powers of two 16 .. 1024 (transform lengths 32 R, R a power of
-// two) and the multiples of 16 from 48 to 240 (R = 3 .. 15: the warp FFT's direct register DFT).
+// two), the multiples of 16 from 48 to 240 (R = 3 .. 15: the warp FFT's direct register DFT), and
+// every other bandwidth from 17 to 255 through chirp-z transforms (czt_split.cu).
 static bool split_bw_ok(int B) {
     if (B < 16 || B > 1024) return false;
     if ((B & (B - 1)) == 0) return true;
-    return B % 16 == 0 && B / 16 <= 15;
+    return (B % 16 == 0 && B / 16 <= 15) || split_czt(B);
 }
 
 static int build_split(Tables* t) {
@@ -337,10 +345,16 @@ static int build_split(Tables* t) {
     const int B = t->bw, S = 2 * B;
     if (!split_bw_ok(B))
         return fail(S2G_ERR_UNSUPPORTED,
-                    "split-precision path needs a power-of-two bw in [16, 1024] or a multiple of 16 in [48, 240] "
-                    "(got %d)",
+                    "split-precision path needs a bw in [16, 256] or a power of two up to 1024 (got %d)",
                     B);
     if (t->cutoff != B) return fail(S2G_ERR_UNSUPPORTED, "split-precision path is seminaive at every order (cutoff == bw)");
+    // every work item's N extent (table rows) must be a valid tcgen05 N: a multiple of 16, at most 256
+    for (int m = 0; m < B; ++m)
+        for (int d = 0; d < 2; ++d) {
+            const Geo g = geo(d == 0, B, m);
+            if (g.NP % 16 || g.NP < 16 || g.KX < 1)
+                return fail(S2G_ERR_UNSUPPORTED, "contraction geometry of bw %d, order %d: N extent %d", B, m, g.NP);
+        }
     Split* s = new Split();
     s->B = B;
     s->KC = kKC;
@@ -374,6 +388,10 @@ static int build_split(Tables* t) {
             k_tw_f32<<<(S + 255) / 256, 256, 0, st>>>(t->tw_D, s->twD, S);
         }
         ck(cudaGetLastError(), "conversion kernels");
+    }
+    if (r == S2G_OK && split_czt(B)) {
+        r = czt_build_tables(B, &s->czh, &s->czK, &s->cztw);
+        if (r == S2G_OK) s->czM = czt_len(B);
     }
     if (r == S2G_OK) r = pack_blobs(t, s, false, st);
     cudaStreamDestroy(st);
@@ -989,13 +1007,14 @@ static constexpr int kMaxClasses = 6;  // bandwidths 16 .. 512
 
 struct LegClass {
     int B, N, ntiles;         // bandwidth, functions, 64-function tiles
+    int BH, BN, SX;           // intermediate layout (SplitLayout): C/Fc half rows, folded halves, X/F rows
     int NB;                   // table rows per work item (N extent of the tile)
     int per_tile;             // work items per 64-function tile
     const int2* itab;         // per_tile entries: (order m, index of the item within the order)
     int64_t item0;            // first work item of the class
     float tab_inv;            // inverse of the table blob's scale
-    const float* C;           // forward seminaive input C[p][f][m][t][j] (k = 2j + t)
-    const float* X;           // forward naive input, folded halves X[p][f][m][t][j], j < B
+    const float* C;           // forward seminaive input C[p][f][m][t][j] (k = 2j + t), rows of 2 BH
+    const float* X;           // forward naive input, folded halves X[p][f][m][t][j], j < B, rows of SX
     const float* rc_in;       // inverse input coefficients
     const float* ic_in;
     float* rc;                // forward output coefficients
@@ -1058,9 +1077,8 @@ __device__ __forceinline__ int64_t coef_base(const LegClass& k, int f) {
 //   inverse          : a(l), l - m = 2i + t, from the coefficient arrays (stride 2)
 template <bool FWD>
 __device__ __forceinline__ const float* fwd_row(const LegClass& k, int m, bool nv, int t, int f, int part) {
-    const int B = k.B;
-    return nv ? k.X + (((size_t)part * k.N + f) * B + m) * (2 * B) + t * B
-              : k.C + (((size_t)part * k.N + f) * B + m) * B + t * (B / 2);
+    const size_t row = ((size_t)part * k.N + f) * k.B + m;
+    return nv ? k.X + row * k.SX + t * k.BN : k.C + row * (2 * k.BH) + t * k.BH;
 }
 
 template <bool FWD>
@@ -1074,7 +1092,7 @@ __device__ __forceinline__ void load_seg(const LegClass& k, int m, bool nv, int 
     }
     const int j0 = c * kKC + seg * 8;
     if (FWD) {
-        if (j0 >= (nv ? B : B / 2)) {
+        if (j0 >= (nv ? k.BN : k.BH)) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) v[q] = 0.f;
             return;
@@ -1199,12 +1217,12 @@ __device__ __forceinline__ void epi_store(const LegClass& K, int m, int t, int n
         }
     } else if (!naive_order(m)) {
         const float sc_ = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
-        const int nj = min(w, B / 2 - c0);
+        const int nj = min(w, (B + 1) / 2 - c0);
         for (int r = wid; r < 128; r += nw) {
             const int f = f0 + (r & 63), part = r >> 6;
             if (f >= K.N) continue;
             const float* src = ep + r * ES;
-            float* dst = K.Fc + (((size_t)part * K.N + f) * B + m) * B + t * (B / 2) + c0;
+            float* dst = K.Fc + (((size_t)part * K.N + f) * B + m) * (2 * K.BH) + t * K.BH + c0;
             for (int j = lane; j < nj; j += 32) dst[j] = src[j] * ((c0 + j + t) == 0 ? sc0 : sc_);
         }
     } else {
@@ -1213,7 +1231,7 @@ __device__ __forceinline__ void epi_store(const LegClass& K, int m, int t, int n
             const int f = f0 + (r & 63), part = r >> 6;
             if (f >= K.N) continue;
             const float* src = ep + r * ES;
-            float* dst = K.F + (((size_t)part * K.N + f) * B + m) * (2 * B) + t * B + nb * NP + c0;
+            float* dst = K.F + (((size_t)part * K.N + f) * B + m) * K.SX + t * K.BN + nb * NP + c0;
             for (int i = lane; i < wn; i += 32) dst[i] = src[i];
         }
     }
@@ -1393,8 +1411,9 @@ __device__ __forceinline__ void issue_chunk(const LegClass& K, const WsItem& e, 
         float4* d0 = stg_at(stg, s, q, 0, tid);
         float4* d1 = stg_at(stg, s, q, 1, tid);
         if (FWD) {
-            // rows are 32-byte aligned: C rows are B/2 floats apart, folded X rows B, and j0 % 8 == 0
-            const bool ok = f < K.N && j0 < (nv ? B : B / 2);
+            // rows are 32-byte aligned: C rows are BH floats apart, folded X rows BN (both multiples
+            // of 8), and j0 % 8 == 0
+            const bool ok = f < K.N && j0 < (nv ? K.BN : K.BH);
             const float* src = ok ? fwd_row<FWD>(K, e.m, nv, e.t, f, part) + j0 : (nv ? K.X : K.C);
             tc::cp_async16(d0, src, ok ? 16u : 0u);
             tc::cp_async16(d1, ok ? src + 4 : src, ok ? 16u : 0u);
@@ -1564,7 +1583,7 @@ __device__ __forceinline__ void produce_a_tma(const Leg& p, uint8_t* smem, const
                 const int j0 = c * kKC + seg * 8;
                 if (FWD) {
                     // 128-byte rows (p, f), 16-byte chunk u of row r stored at chunk u ^ (r % 8)
-                    const bool valid = j0 < (nv ? B : B / 2);
+                    const bool valid = j0 < (nv ? K.BN : K.BH);
                     const float4 a = *reinterpret_cast<const float4*>(sb + r * 128 + (((2 * seg) ^ (r & 7)) << 4));
                     const float4 b = *reinterpret_cast<const float4*>(sb + r * 128 + (((2 * seg + 1) ^ (r & 7)) << 4));
                     va[q][0] = valid ? a.x : 0.f, va[q][1] = valid ? a.y : 0.f;
@@ -1626,7 +1645,7 @@ __device__ __forceinline__ void issue_a_tma(const Leg& p, const WsItem& e, int c
     tc::mbar_arrive_expect_tx(bar, p.a_chunk_bytes);
     if (FWD) {
         const bool nv = naive_order(e.m);
-        const int x = (nv ? e.t * B : e.t * (B / 2)) + c * kKC;
+        const int x = (nv ? e.t * p.cls[0].BN : e.t * p.cls[0].BH) + c * kKC;
         tc::tma_load_4d(dst, nv ? (const void*)&p.tmA1 : (const void*)&p.tmA0, x, e.m, e.f0, 0, bar);
     } else {
         const int x0 = (index_of_harmonic_coeff(e.m, e.m, B) + c * 64) & ~3;
@@ -1977,7 +1996,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                     tc::fence_proxy_async_smem();
                     tc::named_bar_sync(ebar, kEpi);
                     if (et == 0) {
-                        tc::tma_store_4d(&p.tmO, t * (B / 2) + j0, m, e.f0, 0, eb);
+                        tc::tma_store_4d(&p.tmO, t * K.BH + j0, m, e.f0, 0, eb);
                         tc::bulk_commit();
                     }
                 }
@@ -2094,8 +2113,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 
 // ------------------------------------------------------------------------------------
 size_t split_work_bytes(int bw, int batch) {
-    const size_t B = bw, S = 2 * B;
-    return 2 * (size_t)batch * B * (S + B) * sizeof(float) + 1024;
+    const SplitLayout L = split_layout(bw);
+    return 2 * (size_t)batch * bw * ((size_t)L.SX + 2 * (size_t)L.BH) * sizeof(float) + 1024;
 }
 
 static int set_smem(const void* fn, size_t bytes) {
@@ -2305,6 +2324,10 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
         // inverse TMA stores take 32-column blocks, and its staging leaves room for 128-row tables
         if (want_tma && !fwd) NB = std::max(32, std::min(128, NB) & ~31);
         k.B = B;
+        const SplitLayout lay = split_layout(B);
+        k.BH = lay.BH;
+        k.BN = lay.BN;
+        k.SX = lay.SX;
         k.N = q.N;
         k.ntiles = (q.N + 63) / 64;
         k.NB = NB;
@@ -2396,6 +2419,10 @@ static int launch_fft_kernels(int which, const void* in, void* out, int N, const
 
 static int fft_kernels(int which, int B, const void* in, void* out, int N, const Split* s, cudaStream_t st,
                        float scale, const int64_t* gmap = nullptr) {
+    if (s->czM) {
+        const CztTabs g{B, s->czM, s->czh, s->czK, s->cztw, s->w32, s->sin32, s->twD};
+        return czt_stage(which, g, in, out, N, scale, gmap, st);
+    }
     if ((2 * B) % 32) return fail(S2G_ERR_UNSUPPORTED, "no warp FFT for bandwidth %d", B);
     switch (2 * B / 32) {
         case 1: return launch_fft_kernels<1>(which, in, out, N, s, st, scale, gmap);
@@ -2515,7 +2542,8 @@ int split_stage_group(int which, const StageSpec* spec, int ncls, int dct_ctas_p
 
 // Work counter of the contraction kernel: the int after the two intermediate arrays.
 static int* work_counter(void* work, int B, int batch) {
-    const size_t used = 2 * (size_t)batch * B * (3 * B) * sizeof(float);
+    const SplitLayout L = split_layout(B);
+    const size_t used = 2 * (size_t)batch * B * ((size_t)L.SX + 2 * (size_t)L.BH) * sizeof(float);
     return (int*)((char*)work + ((used + 255) & ~(size_t)255));
 }
 
@@ -2528,7 +2556,7 @@ int fst_split(Tables* t, const float* grid, float* rc, float* ic, int batch, int
     Split* s = (Split*)t->split;
     const int B = t->bw, S = 2 * B;
     float* X = (float*)work;
-    float* Cb = X + 2 * (size_t)batch * B * S;
+    float* Cb = X + 2 * (size_t)batch * B * split_layout(B).SX;
     // 1. DFT along phi (two real latitudes per warp), scaled by sqrt(2 pi)/S   (FST_semi_memo.c:81-90)
     S2G_TRY(fft_kernels(0, B, grid, X, batch, s, st, (float)(sqrt(2.0 * kPi) / S)));
     // 2. weighted DCT-II per (function, seminaive order)                      (seminaive.c:161-176)
@@ -2549,9 +2577,9 @@ int inv_fst_split(Tables* t, const float* rc, const float* ic, float* grid, int 
     int nprod = 0;
     bool f16 = false;
     S2G_TRY(check_prec(precision, &nprod, &f16));
-    const int B = t->bw, S = 2 * B;
+    const int B = t->bw;
     float* F = (float*)work;
-    float* Fc = F + 2 * (size_t)batch * B * S;
+    float* Fc = F + 2 * (size_t)batch * B * split_layout(B).SX;
     LegSpec q{};
     q.t = t;
     q.N = batch;

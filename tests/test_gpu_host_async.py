@@ -26,7 +26,7 @@ def _sync_roundtrip(plan, rc, ic, nb):
     return g, orc, oic
 
 
-@pytest.mark.parametrize("bw,nb", [(64, 150), (256, 70)])
+@pytest.mark.parametrize("bw,nb", [(64, 150), (256, 70), (101, 70)])
 def test_async_chain_matches_sync(bw, nb):
     rng = np.random.default_rng(bw + nb)
     plan = api.Plan(bw, bw)

@@ -64,7 +64,10 @@ def _nerr(got, ref):
 @pytest.mark.parametrize("bw,nb", [(16, 3), (32, 70), (64, 10), (128, 65), (256, 130), (512, 2),
                                    # multiples of 16 that are not powers of two (transform lengths
                                    # 32 R, R = 3 .. 15; bw 144 and 240 have a partial naive block)
-                                   (48, 5), (80, 70), (112, 3), (144, 65), (192, 33), (208, 2), (240, 4)])
+                                   (48, 5), (80, 70), (112, 3), (144, 65), (192, 33), (208, 2), (240, 4),
+                                   # chirp-z lengths (odd bw, and even bw that no warp FFT takes), one per
+                                   # convolution length M = 128 .. 1024 at least
+                                   (17, 3), (24, 5), (33, 66), (100, 2), (127, 65), (200, 3), (255, 33)])
 @pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_BF16X2, api.PREC_FP16X2])
 def test_split_forward_inverse_vs_fp64(bw, nb, prec):
     torch = _torch()
@@ -92,11 +95,13 @@ def test_split_forward_inverse_vs_fp64(bw, nb, prec):
     assert e_inv <= tol, e_inv
 
 
-@pytest.mark.parametrize("bw", [96, 192])
+@pytest.mark.parametrize("bw", [96, 192, 31, 101, 255])
 def test_split_non_power_of_two_vs_oracle(oracle, bw):
-    """A bandwidth that is not a power of two (lengths 2 bw = 32 R, R = 6 and 12) on the split
-    path against the oracle directly: forward of the oracle's samples and inverse of the
-    coefficients, BF16X3 tolerance."""
+    """Bandwidths that are not powers of two on the split path against the oracle directly: lengths
+    2 bw = 32 R (R = 6 and 12: the warp FFTs' direct register DFT) and odd bandwidths (chirp-z
+    transforms), forward of the oracle's samples and inverse of the coefficients, BF16X3 tolerance.
+    The reference's own inverse is wrong at odd bw (Transpose_RowSize, cospml.c:270-288); the
+    oracle uses the true row counts and reproduces the reference's odd-bw forward known answers."""
     torch = _torch()
     nb = 2
     rng = np.random.default_rng(bw)
@@ -239,7 +244,7 @@ def test_split_host_api_matches_device_api():
 def test_split_rejects_unsupported():
     import s2kit_gb300 as s2
     torch = _torch()
-    for bw in (24, 200, 272):  # not a power of two, and not a multiple of 16 in [48, 240]
+    for bw in (8, 272, 300):  # below 16, and above 256 without being a power of two
         plan = api.Plan(bw, bw)
         x = torch.zeros(4 * bw * bw, device="cuda")
         with pytest.raises(s2.S2GError):
