@@ -175,6 +175,8 @@ def algorithmic_bytes(kernel, B, N):
         "dct_inv_f32": 2 * N * ns * B * f + 2 * N * ns * S * f + 2 * 2 * N * nn * S * f,
         "rows_inv_f32": 2 * N * B * S * f + N * S * S * f,
     }
+    for name in ("rows_fwd", "dct_fwd", "dct_inv", "rows_inv"):  # chirp-z stages move the same bytes
+        table[name + "_czt"] = table[name + "_f32"]
     return table.get(kernel)
 
 

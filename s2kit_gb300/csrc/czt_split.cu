@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kT) k_czt_rows_fwd(const float* __restrict__ g
 // orders are folded in place in X: X[p][f][m][t BN + j] = x_j + (-1)^t x_(S-1-j), j < B, zeros
 // up to BN.  Persistent: each warp walks rows.
 template <int RM>
-__global__ void __launch_bounds__(kT) k_czt_dct_fwd(float* __restrict__ X, float* __restrict__ Cout, int nrows,
+__global__ void __launch_bounds__(kT, 2) k_czt_dct_fwd(float* __restrict__ X, float* __restrict__ Cout, int nrows,
                                                     int B, int BH, int BN, int SX, const CztTabs g) {
     using Sh = CztShape<RM>;
     constexpr int PSA = Sh::PSA;
@@ -237,17 +237,25 @@ __global__ void __launch_bounds__(kT) k_czt_dct_fwd(float* __restrict__ X, float
             continue;
         }
         const float* ws = w + ((m & 1) ? S : 0);
+        // the weighted row goes through the warp's rows (coalesced loads, few registers in flight),
+        // then into the registers in Makhoul's order
+        for (int q = lane; q < S; q += 32) {
+            zr[q] = xr[q] * ws[q];
+            zi[q] = xi[q] * ws[q];
+        }
+        __syncwarp();
         float2 v[RM];
 #pragma unroll
         for (int i = 0; i < RM; ++i) {
             const int n = lane + 32 * i;
             if (n < S) {
                 const int q = n < B ? 2 * n : 2 * (S - 1 - n) + 1;
-                v[i] = cmulf(make_float2(xr[q] * ws[q], xi[q] * ws[q]), chirp(t, n, -1.f));
+                v[i] = cmulf(make_float2(zr[q], zi[q]), chirp(t, n, -1.f));
             } else {
                 v[i] = make_float2(0.f, 0.f);
             }
         }
+        __syncwarp();  // every lane has read the staged row before the transform reuses the rows
         czt_warp<RM>(v, t, zr, zi, S, -1.f);
         float* cr = Cout + (size_t)row * (2 * BH);
         float* ci = cr + (size_t)nrows * (2 * BH);

@@ -1455,7 +1455,7 @@ __device__ __forceinline__ void produce_a_async(const Leg& p, uint8_t* smem, flo
             if (!have_ei) {
                 const int sl = ki % kNI;
                 const uint32_t ph = (ki / kNI) & 1;
-                if (!__all_sync(full, tc::mbar_try_wait(&item_full[sl], ph))) {
+                if (!__all_sync(full, tc::mbar_test_wait(&item_full[sl], ph))) {
                     if (n_iss != n_con) return true;
                     if (!__all_sync(full, tc::mbar_wait(&item_full[sl], ph))) return false;
                 }
