@@ -1730,6 +1730,13 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             int bs = 0;       // stage of chunk bc (running: no division per chunk)
             uint32_t bph = 0; // its phase parity
             WsItem odd{};     // parity pairs: the odd item of the pair fetched at the last even k
+            // The next claim on the work counter is issued before the current item's table copies,
+            // so the atomic's round trip overlaps them (its result is read only when the next item
+            // is decoded).  Item tables list the parities of an (order, block) next to each other
+            // and every class holds an even number of items, so in pair mode an even index starts a
+            // pair and one claim takes both.
+            const int claim = p.pair ? 2 : 1;
+            long long next_idx = p.stall ? 0 : atomicAdd(p.counter, claim);
             for (int k = 0; !s_abort && !p.stall; ++k) {
                 const int slot = k % kNI;
                 if (!tc::mbar_wait(&item_empty[slot], ((k / kNI) & 1) ^ 1)) {
@@ -1737,14 +1744,14 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                     break;
                 }
                 WsItem e;
+                bool claimed = false;
                 if (p.pair && (k & 1)) {
                     e = odd;
                 } else {
-                    // item tables list the parities of an (order, block) next to each other and every
-                    // class holds an even number of items, so an even index starts a pair
-                    const long long idx = atomicAdd(p.counter, p.pair ? 2 : 1);
+                    const long long idx = next_idx;
                     e = decode_item<FWD>(p, idx);
                     if (p.pair) odd = decode_item<FWD>(p, idx + 1);
+                    claimed = true;
                 }
                 items[slot] = e;
                 tc::mbar_arrive(&item_full[slot]);
@@ -1763,6 +1770,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                     }
                     break;
                 }
+                if (claimed) next_idx = atomicAdd(p.counter, claim);
                 const LegClass& K = p.cls[e.ci];
                 const Geo g = geo(FWD, K.B, e.m);
                 const int n0 = e.sub * K.NB, rows = min(K.NB, g.NP - n0);
