@@ -2647,17 +2647,19 @@ __global__ void __launch_bounds__(256) k_cplx_combine(const float* __restrict__ 
                                                       const float* __restrict__ hr, const float* __restrict__ hi,
                                                       float* __restrict__ rc, float* __restrict__ ic, int B,
                                                       long long nquads) {
-    const int BB = B * B, qpf = BB / 4;
+    const int BB = B * B, qpf = (BB + 3) / 4;  // quads per function, the last partial when 4 does not divide B^2
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nquads;
          q += (long long)gridDim.x * blockDim.x) {
         const long long f = q / qpf;
         const int j0 = 4 * (int)(q - f * qpf);
+        const int ne = min(4, BB - j0);
         const size_t base = (size_t)f * BB;
         int m, l;
         coeff_order_degree(j0, B, &m, &l);
-        float orr[4], oi[4];
+        float orr[4] = {0.f, 0.f, 0.f, 0.f}, oi[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
+            if (e >= ne) break;
             const int am = m >= 0 ? m : -m;
             const size_t src = base + am * B - (am * (am - 1)) / 2 + (l - am);
             const float a = __ldg(gr + src), b = __ldg(gi + src), c = __ldg(hr + src), d = __ldg(hi + src);
@@ -2671,8 +2673,15 @@ __global__ void __launch_bounds__(256) k_cplx_combine(const float* __restrict__ 
             }
             coeff_next(B, &m, &l);
         }
-        *(float4*)(rc + base + j0) = make_float4(orr[0], orr[1], orr[2], orr[3]);
-        *(float4*)(ic + base + j0) = make_float4(oi[0], oi[1], oi[2], oi[3]);
+        if ((BB & 3) == 0) {  // every function starts 16-byte aligned, every quad is whole
+            *(float4*)(rc + base + j0) = make_float4(orr[0], orr[1], orr[2], orr[3]);
+            *(float4*)(ic + base + j0) = make_float4(oi[0], oi[1], oi[2], oi[3]);
+        } else {
+            for (int e = 0; e < ne; ++e) {
+                rc[base + j0 + e] = orr[e];
+                ic[base + j0 + e] = oi[e];
+            }
+        }
     }
 }
 
@@ -2683,19 +2692,32 @@ __global__ void __launch_bounds__(256) k_cplx_split(const float* __restrict__ rc
                                                     float* __restrict__ gr, float* __restrict__ gi,
                                                     float* __restrict__ hr, float* __restrict__ hi, int B,
                                                     long long nquads) {
-    const int BB = B * B, nn = B * (B + 1) / 2, qpf = nn / 4;
+    // quads of the non-negative orders per function (the last partial when 4 does not divide nn)
+    const int BB = B * B, nn = B * (B + 1) / 2, qpf = (nn + 3) / 4;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nquads;
          q += (long long)gridDim.x * blockDim.x) {
         const long long f = q / qpf;
         const int j0 = 4 * (int)(q - f * qpf);
+        const int ne = min(4, nn - j0);
         const size_t base = (size_t)f * BB;
+        const bool vec = (BB & 3) == 0 && ne == 4;  // a whole quad at a 16-byte aligned position
         int m, l;
         coeff_order_degree(j0, B, &m, &l);
-        const float4 ar = *(const float4*)(rc + base + j0), ai = *(const float4*)(ic + base + j0);
-        const float far_[4] = {ar.x, ar.y, ar.z, ar.w}, fai[4] = {ai.x, ai.y, ai.z, ai.w};
+        float far_[4] = {0.f, 0.f, 0.f, 0.f}, fai[4] = {0.f, 0.f, 0.f, 0.f};
+        if (vec) {
+            const float4 ar = *(const float4*)(rc + base + j0), ai = *(const float4*)(ic + base + j0);
+            far_[0] = ar.x, far_[1] = ar.y, far_[2] = ar.z, far_[3] = ar.w;
+            fai[0] = ai.x, fai[1] = ai.y, fai[2] = ai.z, fai[3] = ai.w;
+        } else {
+            for (int e = 0; e < ne; ++e) {
+                far_[e] = rc[base + j0 + e];
+                fai[e] = ic[base + j0 + e];
+            }
+        }
         float o[4][4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
+            if (e >= ne) break;
             const int L = B - 1;
             const size_t neg = m == 0 ? base + j0 + e
                                       : base + (L * (L + 3)) / 2 + 1 + ((L - m) * (L - m + 1)) / 2 + (l - m);
@@ -2707,10 +2729,19 @@ __global__ void __launch_bounds__(256) k_cplx_split(const float* __restrict__ rc
             o[3][e] = -0.5f * (far_[e] - br);
             coeff_next(B, &m, &l);
         }
-        *(float4*)(gr + base + j0) = make_float4(o[0][0], o[0][1], o[0][2], o[0][3]);
-        *(float4*)(gi + base + j0) = make_float4(o[1][0], o[1][1], o[1][2], o[1][3]);
-        *(float4*)(hr + base + j0) = make_float4(o[2][0], o[2][1], o[2][2], o[2][3]);
-        *(float4*)(hi + base + j0) = make_float4(o[3][0], o[3][1], o[3][2], o[3][3]);
+        if (vec) {
+            *(float4*)(gr + base + j0) = make_float4(o[0][0], o[0][1], o[0][2], o[0][3]);
+            *(float4*)(gi + base + j0) = make_float4(o[1][0], o[1][1], o[1][2], o[1][3]);
+            *(float4*)(hr + base + j0) = make_float4(o[2][0], o[2][1], o[2][2], o[2][3]);
+            *(float4*)(hi + base + j0) = make_float4(o[3][0], o[3][1], o[3][2], o[3][3]);
+        } else {
+            for (int e = 0; e < ne; ++e) {
+                gr[base + j0 + e] = o[0][e];
+                gi[base + j0 + e] = o[1][e];
+                hr[base + j0 + e] = o[2][e];
+                hi[base + j0 + e] = o[3][e];
+            }
+        }
     }
 }
 
@@ -2732,7 +2763,7 @@ int fst_split_complex(Tables* t, const float* rgrid, const float* igrid, float* 
     float* h = g + 2 * n;
     S2G_TRY(fst_split(t, rgrid, g, g + n, batch, precision, work, st));
     S2G_TRY(fst_split(t, igrid, h, h + n, batch, precision, work, st));
-    const long long nq = (long long)n / 4;
+    const long long nq = (long long)batch * ((B * B + 3) / 4);  // quads per function, see k_cplx_combine
     int grid;
     S2G_TRY(launch_grid_stride(nq, &grid));
     ProfScope ps_("cplx_combine", st);
@@ -2750,7 +2781,7 @@ int inv_fst_split_complex(Tables* t, const float* rc, const float* ic, float* rg
     const size_t n = (size_t)batch * B * B;
     float* g = (float*)cwork;
     float* h = g + 2 * n;
-    const long long nq = (long long)batch * (B * (B + 1) / 2) / 4;
+    const long long nq = (long long)batch * ((B * (B + 1) / 2 + 3) / 4);  // see k_cplx_split
     int grid;
     S2G_TRY(launch_grid_stride(nq, &grid));
     {

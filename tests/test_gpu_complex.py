@@ -47,7 +47,7 @@ def _run(plan, gr, gi, cr, ci, nb, prec):
     return [x.double().cpu().numpy() for x in (o_r, o_i, s_r, s_i)]
 
 
-@pytest.mark.parametrize("bw,nb", [(16, 3), (32, 2)])
+@pytest.mark.parametrize("bw,nb", [(16, 3), (32, 2), (33, 2)])  # bw 33: chirp-z stages
 @pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_BF16X2, api.PREC_FP16X2])
 def test_split_complex_vs_oracle(oracle, bw, nb, prec):
     rng = np.random.default_rng(1000 + bw)
@@ -83,7 +83,7 @@ def test_split_complex_reference_fixture(golden):
                         g["fwd_noise_i"]) <= 1e-6
 
 
-@pytest.mark.parametrize("bw,nb", [(128, 5), (256, 3), (512, 2)])
+@pytest.mark.parametrize("bw,nb", [(128, 5), (256, 3), (512, 2), (101, 3)])
 def test_split_complex_vs_fp64_path(bw, nb):
     torch = _torch()
     rng = np.random.default_rng(7 + bw)

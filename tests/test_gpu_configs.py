@@ -80,12 +80,13 @@ def test_bw1024_fp64_roundtrip_and_conv():
 
 
 @pytest.mark.parametrize("prec", [api.PREC_BF16X3])
-def test_bw1024_split_with_fp64_residual_refinement(prec):
-    """16 real functions at bw 1024: the split path alone, then with one FP64-residual refinement
-    step (forward and inverse) to <= 1e-10 against the FP64 path."""
+@pytest.mark.parametrize("bw,nb", [(1024, 16), (255, 8)])
+def test_split_with_fp64_residual_refinement(bw, nb, prec):
+    """16 real functions at bw 1024 (and 8 at the odd bw 255, whose split stages are chirp-z
+    transforms): the split path alone, then with one FP64-residual refinement step (forward and
+    inverse) to <= 1e-10 against the FP64 path."""
     import torch
-    bw, nb = 1024, 16
-    rng = np.random.default_rng(15)
+    rng = np.random.default_rng(15 + bw)
     rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
     plan = api.Plan(bw, bw)
     d_rc, d_ic = torch.from_numpy(rc).cuda(), torch.from_numpy(ic).cuda()
@@ -115,7 +116,7 @@ def test_bw1024_split_with_fp64_residual_refinement(prec):
     b_rc, b_ic = torch.empty_like(d_rc), torch.empty_like(d_ic)
     plan.fst(r_grid, None, b_rc, b_ic, nb, api.REAL)
     e_inv_band = (torch.hypot(b_rc - f_rc, b_ic - f_ic).amax(1) / mag).max().item()
-    print(f"bw 1024: split {e_split:.2e}, refined forward {e_fwd:.2e}, refined inverse {e_inv:.2e} pointwise, "
+    print(f"bw {bw}: split {e_split:.2e}, refined forward {e_fwd:.2e}, refined inverse {e_inv:.2e} pointwise, "
           f"{e_inv_band:.2e} band-limited")
     assert e_fwd <= 1e-10, e_fwd
     assert e_inv_band <= 1e-10, e_inv_band
