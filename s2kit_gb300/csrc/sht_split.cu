@@ -1203,36 +1203,67 @@ __device__ __forceinline__ void epi_store(const LegClass& K, int m, int t, int n
         const int nbase = index_of_harmonic_coeff(-m, m, B) + t + 2 * c0;
         const int nv_ = min(w, nr_par(B, m, t) - c0);
         const float sgn = (m & 1) ? -1.f : 1.f;
-        for (int r = wid; r < 128; r += nw) {
-            const int f = f0 + (r & 63), part = r >> 6;
-            if (f >= K.N) continue;
-            const float* src = ep + r * ES;
-            float* out = (part ? K.ic : K.rc) + coef_base(K, f);
-            const float s2 = part ? -sgn : sgn;
-            for (int i = lane; i < nv_; i += 32) {
-                const float v = src[i];
-                out[base + 2 * i] = v;
-                if (m) out[nbase + 2 * i] = s2 * v;
+        // Rows in groups of RU per warp: all of a group's shared-memory loads are issued before
+        // its global stores.  The staging tile is reached through a generic pointer, so a load
+        // placed after a global store waits for that store's address to be resolved; loads that
+        // go first overlap their latencies.  Two values per lane cover a row (w <= 64).
+        constexpr int RU = 4;
+        for (int r0 = wid; r0 < 128; r0 += RU * nw) {
+            float v[RU][2];
+#pragma unroll
+            for (int u = 0; u < RU; ++u) {
+                const int r = r0 + u * nw;
+                const float* src = ep + (r < 128 ? r : 0) * ES;
+                v[u][0] = lane < nv_ ? src[lane] : 0.f;
+                v[u][1] = lane + 32 < nv_ ? src[lane + 32] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < RU; ++u) {
+                const int r = r0 + u * nw;
+                const int f = f0 + (r & 63), part = r >> 6;
+                if (r >= 128 || f >= K.N) continue;
+                float* out = (part ? K.ic : K.rc) + coef_base(K, f);
+                const float s2 = part ? -sgn : sgn;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int i = lane + 32 * h;
+                    if (i < nv_) {
+                        out[base + 2 * i] = v[u][h];
+                        if (m) out[nbase + 2 * i] = s2 * v[u][h];
+                    }
+                }
             }
         }
-    } else if (!naive_order(m)) {
-        const float sc_ = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
-        const int nj = min(w, (B + 1) / 2 - c0);
-        for (int r = wid; r < 128; r += nw) {
-            const int f = f0 + (r & 63), part = r >> 6;
-            if (f >= K.N) continue;
-            const float* src = ep + r * ES;
-            float* dst = K.Fc + (((size_t)part * K.N + f) * B + m) * (2 * K.BH) + t * K.BH + c0;
-            for (int j = lane; j < nj; j += 32) dst[j] = src[j] * ((c0 + j + t) == 0 ? sc0 : sc_);
-        }
     } else {
-        const int wn = min(w, B - nb * NP - c0);  // latitudes of a partial last block end at B
-        for (int r = wid; r < 128; r += nw) {
-            const int f = f0 + (r & 63), part = r >> 6;
-            if (f >= K.N) continue;
-            const float* src = ep + r * ES;
-            float* dst = K.F + (((size_t)part * K.N + f) * B + m) * K.SX + t * K.BN + nb * NP + c0;
-            for (int i = lane; i < wn; i += 32) dst[i] = src[i];
+        // inverse: Fcos of a seminaive order (scaled), or a naive order's latitude block; rows in
+        // groups of RU as in the forward
+        const bool nv = naive_order(m);
+        const float sc_ = (float)(0.5 / sqrt((double)B)), sc0 = (float)(1.0 / sqrt(2.0 * B));
+        const int nj = nv ? min(w, B - nb * NP - c0)  // latitudes of a partial last block end at B
+                          : min(w, (B + 1) / 2 - c0);
+        constexpr int RU = 4;
+        for (int r0 = wid; r0 < 128; r0 += RU * nw) {
+            float v[RU][2];
+#pragma unroll
+            for (int u = 0; u < RU; ++u) {
+                const int r = r0 + u * nw;
+                const float* src = ep + (r < 128 ? r : 0) * ES;
+                v[u][0] = lane < nj ? src[lane] : 0.f;
+                v[u][1] = lane + 32 < nj ? src[lane + 32] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < RU; ++u) {
+                const int r = r0 + u * nw;
+                const int f = f0 + (r & 63), part = r >> 6;
+                if (r >= 128 || f >= K.N) continue;
+                const size_t row = ((size_t)part * K.N + f) * B + m;
+                float* dst = nv ? K.F + row * K.SX + t * K.BN + nb * NP + c0 : K.Fc + row * (2 * K.BH) + t * K.BH + c0;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int j = lane + 32 * h;
+                    if (j < nj) dst[j] = nv ? v[u][h] : v[u][h] * ((c0 + j + t) == 0 ? sc0 : sc_);
+                }
+            }
         }
     }
 }
@@ -1248,13 +1279,23 @@ __device__ __forceinline__ void epi_store_pair(const LegClass& K, int m, int f0,
     const int base = index_of_harmonic_coeff(m, m, B) + 2 * i0 + lane;
     const int nbase = index_of_harmonic_coeff(-m, m, B) + 2 * i0 + lane;
     const float sgn = (m & 1) ? -1.f : 1.f;
-    for (int r = wid; r < 128; r += nw) {
-        const int f = f0 + (r & 63), part = r >> 6;
-        if (f >= K.N) continue;
-        const float v = ep[r * ES + lane];
-        float* out = (part ? K.ic : K.rc) + coef_base(K, f);
-        out[base] = v;
-        if (m) out[nbase] = (part ? -sgn : sgn) * v;
+    constexpr int RU = 4;  // rows per group: the group's shared-memory loads go before its stores (see epi_store)
+    for (int r0 = wid; r0 < 128; r0 += RU * nw) {
+        float v[RU];
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+            const int r = r0 + u * nw;
+            v[u] = ep[(r < 128 ? r : 0) * ES + lane];
+        }
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+            const int r = r0 + u * nw;
+            const int f = f0 + (r & 63), part = r >> 6;
+            if (r >= 128 || f >= K.N) continue;
+            float* out = (part ? K.ic : K.rc) + coef_base(K, f);
+            out[base] = v[u];
+            if (m) out[nbase] = (part ? -sgn : sgn) * v[u];
+        }
     }
 }
 
@@ -1295,6 +1336,7 @@ static constexpr int kNI = 4;          // item ring entries
 static constexpr int kNAS = 2;         // A stages
 static constexpr int kMaxNBS = 8;      // table stages (upper bound)
 static constexpr int kEpiCols = 64;    // epilogue staging width
+static_assert(kEpiCols <= 64, "epi_store holds two staged values per lane and row");
 static constexpr int kMaxStg = 8;      // FP32 staging stages of the BF16 A producers (upper bound)
 static constexpr int kAProd = 256;     // A-producer threads
 static constexpr int kEpi = 128;       // epilogue threads
@@ -1967,9 +2009,14 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                         tc::tc_fence_before();
                         tc::mbar_arrive(&acc_empty[buf]);
                     }
+                    // the even parity's 16 values are read before any store (generic pointers:
+                    // a load after a store would wait for it)
+                    float ev[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) ev[q] = stash[et * SST + cb0 + q];
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
-                        ep[et * PS + 2 * q] = stash[et * SST + cb0 + q];
+                        ep[et * PS + 2 * q] = ev[q];
                         ep[et * PS + 2 * q + 1] = v[q] * rs;
                     }
                     tc::named_bar_sync(ebar, kEpi);
