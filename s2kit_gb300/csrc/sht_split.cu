@@ -1026,7 +1026,7 @@ struct LegClass {
     const int64_t* blob_off;
 };
 
-// Tensor-map TMA path (one bandwidth class, BF16 terms, no coefficient map, bw >= 64): the A
+// Tensor-map TMA path (one bandwidth class, BF16 terms, no coefficient map, bw a multiple of 64): the A
 // operand of every chunk is one or two tiled TMA loads into a staging ring, and the inverse's
 // seminaive output leaves through tiled TMA stores.  Boxes (innermost first):
 //   forward seminaive: C      [p][f][m][t*B/2 + j]  box {32, 1, 64, 2}, 128-byte swizzle
@@ -2364,10 +2364,11 @@ int split_leg(bool fwd, int precision, const LegSpec* spec, int ncls, int* count
     p.stall = g_leg_stall.load();
     long long items = 0;
     int nbmax = 16;
-    // tensor-map TMA path: one class, BF16 terms, contiguous batches, bw >= 64, warp-specialised kernel
-    // (power-of-two bw: the inverse's 32-column output boxes then never reach into the other parity)
-    const bool want_tma = g_leg_tma && !f16 && ncls == 1 && !spec[0].cmap &&
-                          spec[0].t->bw >= 64 && (spec[0].t->bw & (spec[0].t->bw - 1)) == 0;
+    // tensor-map TMA path: one class, BF16 terms, contiguous batches, bw a multiple of 64 (the
+    // inverse's 32-column output boxes then never reach into the other parity's half row, and every
+    // row of the maps is a multiple of 16 bytes), warp-specialised kernel
+    const bool want_tma = g_leg_tma && !f16 && ncls == 1 && !spec[0].cmap && spec[0].t->bw >= 64 &&
+                          spec[0].t->bw % 64 == 0;
     for (int c = 0; c < ncls; ++c) {
         const LegSpec& q = spec[c];
         S2G_TRY(f16 ? build_split16(q.t) : build_split(q.t));

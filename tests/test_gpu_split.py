@@ -254,7 +254,7 @@ def test_split_rejects_unsupported():
         plan64.fst_real_f32(x, x, x, 1, 7)  # unknown precision
 
 
-@pytest.mark.parametrize("bw,nb", [(16, 70), (64, 130), (256, 64), (512, 3)])
+@pytest.mark.parametrize("bw,nb", [(16, 70), (64, 130), (192, 33), (256, 64), (512, 3)])
 @pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_FP16X2])
 def test_contraction_kernels_agree_bitwise(bw, nb, prec):
     """The warp-specialised kernel's two data paths (tensor-map TMA and per-thread cp.async) do the
