@@ -95,6 +95,29 @@ def test_split_forward_inverse_vs_fp64(bw, nb, prec):
     assert e_inv <= tol, e_inv
 
 
+@pytest.mark.parametrize("bw", list(range(16, 257, 13)))
+def test_split_bandwidth_sweep_vs_fp64(bw):
+    """Every 13th bandwidth from 16 to 250 (odd and even, warp-FFT and chirp-z lengths, full and
+    partial naive blocks): two functions forward and inverse in BF16X3 against the FP64 path."""
+    torch = _torch()
+    nb = 2
+    rng = np.random.default_rng(1000 + bw)
+    rc, ic = real_field_coeffs(rng, bw, 1.0, nfunc=nb)
+    plan = api.Plan(bw, bw)
+    grid64, frc64, fic64 = _fp64_pair(plan, rc, ic)
+    s_rc = torch.full((nb, bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+    s_ic = torch.full_like(s_rc, float("nan"))
+    plan.fst_real_f32(grid64.float(), s_rc, s_ic, nb, api.PREC_BF16X3)
+    s_grid = torch.full((nb, 4 * bw * bw), float("nan"), dtype=torch.float32, device="cuda")
+    plan.inv_fst_real_f32(torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda(), s_grid, nb,
+                          api.PREC_BF16X3)
+    plan.sync_status()
+    ref_mag = torch.hypot(frc64, fic64).amax(dim=1)
+    e_fwd = (torch.hypot(s_rc.double() - frc64, s_ic.double() - fic64).amax(dim=1) / ref_mag).max().item()
+    e_inv = _nerr(s_grid, grid64)
+    assert e_fwd <= TOL[api.PREC_BF16X3] and e_inv <= TOL[api.PREC_BF16X3], (e_fwd, e_inv)
+
+
 @pytest.mark.parametrize("bw", [96, 192, 31, 101, 255])
 def test_split_non_power_of_two_vs_oracle(oracle, bw):
     """Bandwidths that are not powers of two on the split path against the oracle directly: lengths
