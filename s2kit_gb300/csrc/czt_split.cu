@@ -21,6 +21,9 @@
 #include <math.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "s2g_common.cuh"
@@ -446,12 +449,29 @@ size_t czt_smem(int which, int B) {
     }
 }
 
+// Grid of a persistent stage kernel: the CTAs that fit on the GPU at once, at most `blocks`
+// (resident CTAs cached per device, kernel and shared-memory size).
 int grid_for(const void* fn, size_t smem, long long blocks, int* g) {
-    int occ = 0, dev = 0, nsm = 0;
-    S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kT, smem));
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void*, size_t>, int> cache;
+    int dev = 0;
     S2G_CUDA(cudaGetDevice(&dev));
-    S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    *g = (int)std::max<long long>(1, std::min<long long>(blocks, (long long)std::max(occ, 1) * nsm));
+    const auto key = std::make_tuple(dev, fn, smem);
+    int per_gpu = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) per_gpu = it->second;
+    }
+    if (!per_gpu) {
+        int occ = 0, nsm = 0;
+        S2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kT, smem));
+        S2G_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        per_gpu = std::max(occ, 1) * nsm;
+        std::lock_guard<std::mutex> lk(mu);
+        cache[key] = per_gpu;
+    }
+    *g = (int)std::max<long long>(1, std::min<long long>(blocks, per_gpu));
     return S2G_OK;
 }
 
