@@ -96,9 +96,11 @@ def test_split_forward_inverse_vs_fp64(bw, nb, prec):
 
 
 @pytest.mark.parametrize("bw", list(range(16, 257, 13)))
-def test_split_bandwidth_sweep_vs_fp64(bw):
+@pytest.mark.parametrize("prec", [api.PREC_BF16X3, api.PREC_FP16X2])
+def test_split_bandwidth_sweep_vs_fp64(bw, prec):
     """Every 13th bandwidth from 16 to 250 (odd and even, warp-FFT and chirp-z lengths, full and
-    partial naive blocks): two functions forward and inverse in BF16X3 against the FP64 path."""
+    partial naive blocks): two functions forward and inverse against the FP64 path, BF16X3 and
+    FP16X2 at their stated tolerances."""
     torch = _torch()
     nb = 2
     rng = np.random.default_rng(1000 + bw)
@@ -107,15 +109,15 @@ def test_split_bandwidth_sweep_vs_fp64(bw):
     grid64, frc64, fic64 = _fp64_pair(plan, rc, ic)
     s_rc = torch.full((nb, bw * bw), float("nan"), dtype=torch.float32, device="cuda")
     s_ic = torch.full_like(s_rc, float("nan"))
-    plan.fst_real_f32(grid64.float(), s_rc, s_ic, nb, api.PREC_BF16X3)
+    plan.fst_real_f32(grid64.float(), s_rc, s_ic, nb, prec)
     s_grid = torch.full((nb, 4 * bw * bw), float("nan"), dtype=torch.float32, device="cuda")
     plan.inv_fst_real_f32(torch.from_numpy(rc).float().cuda(), torch.from_numpy(ic).float().cuda(), s_grid, nb,
-                          api.PREC_BF16X3)
+                          prec)
     plan.sync_status()
     ref_mag = torch.hypot(frc64, fic64).amax(dim=1)
     e_fwd = (torch.hypot(s_rc.double() - frc64, s_ic.double() - fic64).amax(dim=1) / ref_mag).max().item()
     e_inv = _nerr(s_grid, grid64)
-    assert e_fwd <= TOL[api.PREC_BF16X3] and e_inv <= TOL[api.PREC_BF16X3], (e_fwd, e_inv)
+    assert e_fwd <= TOL[prec] and e_inv <= TOL[prec], (e_fwd, e_inv)
 
 
 @pytest.mark.parametrize("bw", [96, 192, 31, 101, 255])
