@@ -288,14 +288,16 @@ int s2g_plan_wait(s2g_plan plan);
 int s2g_plan_sync_status(s2g_plan plan);
 
 /* Grouped transforms of many real functions of uneven bandwidth (no counterpart in the
- * reference, which transforms one function per call).  Function f has bandwidth bw[f], a power
- * of two in [16, 512]; precision is a split mode (S2G_PREC_BF16X3, _BF16X2 or _FP16X2).  Layout
+ * reference, which transforms one function per call).  Function f has bandwidth bw[f], any
+ * bandwidth of the split path (16 .. 256, or a power of two up to 512), at most 16 distinct ones
+ * per group; precision is a split mode (S2G_PREC_BF16X3, _BF16X2 or _FP16X2).  Layout
  * on the device: the functions back to back in the order given, function f's grid taking
  * (2 bw[f])^2 floats and its coefficients bw[f]^2 floats in each of rcoeffs/icoeffs (the
  * reference layout per function, negative orders written by symmetry as s2g_fst_real_f32);
  * s2g_group_layout returns the offsets.  A call runs each phi-FFT and DCT stage as at most two
- * grouped launches over all bandwidth classes (short transforms, bw <= 64, and long ones, run
- * concurrently) and ONE persistent tensor-core contraction launch over all classes; the sequence
+ * grouped launches over the power-of-two classes (short transforms, bw <= 64, and long ones, run
+ * concurrently) plus one launch per other class, and ONE persistent tensor-core contraction
+ * launch over all classes; the sequence
  * is captured as a CUDA graph on the first call with a given set of pointers and replayed on later
  * calls with the same pointers.  Calls on one group must be serialised (they share the group's
  * intermediate buffers). */

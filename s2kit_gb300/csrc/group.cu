@@ -1,18 +1,21 @@
 // group.cu -- grouped real-field transforms of many functions of uneven bandwidth.
 //
-// A group fixes a list of functions (function f has bandwidth bw[f], a power of two in
-// [16, 512]) and a split precision.  Functions are binned by bandwidth into classes; each
-// class owns class-contiguous intermediate arrays.  One transform runs as
+// A group fixes a list of functions (function f has bandwidth bw[f]: any bandwidth of the split
+// path, i.e. 16 .. 256 or a power of two up to 512, at most 16 distinct ones) and a split
+// precision.  Functions are binned by bandwidth into classes; each class owns class-contiguous
+// intermediate arrays (split_layout).  One transform runs as
 //   forward : the phi-DFT of the classes (FST_semi_memo.c:81-90), then their weighted DCT-II
 //             (seminaive.c:161-176), then ONE persistent tcgen05 contraction launch over the work
 //             items of every class (seminaive.c:183-197);
 //   inverse : ONE persistent contraction launch (seminaive.c:74-98), then the DCT-III with the
 //             naive-order recombination, then the DFT over the orders (FST_semi_memo.c:334-350).
-// Each FFT stage is a grouped launch (k_stage_group: a block decodes its class and runs that
-// class's transform length) over a tier of classes: the short transforms (bw <= 64), compiled
-// for the per-length kernels' small register budgets, and the long ones (bw >= 128).  The two
-// tiers run concurrently on two streams, so a stage is at most two launches whatever the number
-// of classes.  The sequence is captured once as a CUDA graph (on an internal stream, the tiers as
+// Each FFT stage of the power-of-two classes is a grouped launch (k_stage_group: a block decodes
+// its class and runs that class's transform length) over a tier of classes: the short transforms
+// (bw <= 64), compiled for the per-length kernels' small register budgets, and the long ones
+// (bw >= 128).  The two tiers run concurrently on two streams, so those classes take at most two
+// launches per stage whatever their number.  A class of another bandwidth (transform length 32 R
+// with R not a power of two, or a chirp-z length) runs each stage as its own launch on the
+// long tier's stream.  The sequence is captured once as a CUDA graph (on an internal stream, the tiers as
 // parallel branches) and replayed on the caller's stream; the first call with a given set of
 // pointers runs eagerly and captures, later calls replay.
 //
@@ -35,7 +38,10 @@
 
 namespace s2g {
 
-static constexpr int kGroupMaxClasses = 6;
+static constexpr int kGroupMaxClasses = 16;
+
+// Bandwidths whose FFT stages the grouped stage kernel runs (transform lengths 32 R, R a power of two).
+static bool stage_groupable(int B) { return B >= 16 && B <= 512 && (B & (B - 1)) == 0; }
 
 struct GroupClass {
     int B = 0, N = 0, NB = 0;
@@ -43,8 +49,8 @@ struct GroupClass {
     std::vector<int> funcs;     // member functions, in the caller's order
     int64_t* gmap = nullptr;    // device: member i -> grid offset (elements)
     int64_t* cmap = nullptr;    // device: member i -> coefficient offset
-    float* buf0 = nullptr;      // X (forward) / F (inverse): [2][N][B][2B]
-    float* buf1 = nullptr;      // C (forward) / Fc (inverse): [2][N][B][B]
+    float* buf0 = nullptr;      // X (forward) / F (inverse): [2][N][B][SX]  (split_layout)
+    float* buf1 = nullptr;      // C (forward) / Fc (inverse): [2][N][B][2 BH]
 };
 
 struct GroupGraph {
@@ -90,6 +96,7 @@ static int group_stages(s2g_group g, const int* which, int nstage, In in, Out ou
         nlo = nhi = 0;
         for (int c = 0; c < nc; ++c) {
             GroupClass& k = g->cls[c];
+            if (!stage_groupable(k.B)) continue;
             const bool rows = which[w] == 0 || which[w] == 3;
             const StageSpec q{k.t, k.N, in(w, c), out(w, c), rows ? k.gmap : nullptr};
             if (k.B <= kShortTierMaxBw) lo[nlo++] = q;
@@ -102,6 +109,12 @@ static int group_stages(s2g_group g, const int* which, int nstage, In in, Out ou
         const int dc = (which[w] == 1 || which[w] == 2) ? g->dct_ctas : 0;
         if (nhi) S2G_TRY(split_stage_group(which[w], hi, nhi, dc, st));
         if (nlo) S2G_TRY(split_stage_group(which[w], lo, nlo, dc, nhi ? g->side : st));
+        // the other classes: one launch each, in stage order on st
+        for (int c = 0; c < nc; ++c) {
+            GroupClass& k = g->cls[c];
+            if (stage_groupable(k.B)) continue;
+            S2G_TRY(split_stage_one(which[w], k.t, k.N, in(w, c), out(w, c), k.gmap, st));
+        }
     }
     if (nlo && nhi) {
         S2G_CUDA(cudaEventRecord(g->join, g->side));
@@ -416,9 +429,16 @@ int s2g_group_create(s2g_group* out, int nfunc, const int* bw, int precision) {
     if (precision != S2G_PREC_BF16X3 && precision != S2G_PREC_BF16X2 && precision != S2G_PREC_FP16X2)
         return fail(S2G_ERR_ARG, "precision %d is not a split (tensor-core) mode", precision);
     for (int f = 0; f < nfunc; ++f)
-        if (bw[f] < 16 || bw[f] > 512 || (bw[f] & (bw[f] - 1)))
-            return fail(S2G_ERR_UNSUPPORTED, "function %d: bandwidth %d is not a power of two in [16, 512]", f,
-                        bw[f]);
+        if (bw[f] < 16 || bw[f] > 512 || (bw[f] > 256 && (bw[f] & (bw[f] - 1))))
+            return fail(S2G_ERR_UNSUPPORTED,
+                        "function %d: bandwidth %d is neither in [16, 256] nor a power of two up to 512", f, bw[f]);
+    {
+        std::vector<int> distinct(bw, bw + nfunc);
+        std::sort(distinct.begin(), distinct.end());
+        const long nd = std::unique(distinct.begin(), distinct.end()) - distinct.begin();
+        if (nd > kGroupMaxClasses)
+            return fail(S2G_ERR_UNSUPPORTED, "%ld distinct bandwidths in one group (at most %d)", nd, kGroupMaxClasses);
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return fail(S2G_ERR_NOGPU, "no CUDA device");
     s2g_group g = new s2g_group_s();
@@ -435,7 +455,7 @@ int s2g_group_create(s2g_group* out, int nfunc, const int* bw, int precision) {
         g->coef_total += (int64_t)bw[f] * bw[f];
     }
     // classes in increasing bandwidth
-    for (int B = 16; B <= 512; B *= 2) {
+    for (int B = 16; B <= 512; ++B) {
         GroupClass c;
         c.B = B;
         for (int f = 0; f < nfunc; ++f)
@@ -452,9 +472,11 @@ int s2g_group_create(s2g_group* out, int nfunc, const int* bw, int precision) {
     // device memory: maps, intermediates (256-byte aligned pieces), two counters
     auto rnd = [](size_t x) { return (x + 255) & ~(size_t)255; };
     size_t total = 256;
+    auto x_floats = [](const GroupClass& c) { return 2 * (size_t)c.N * c.B * split_layout(c.B).SX; };
+    auto c_floats = [](const GroupClass& c) { return 2 * (size_t)c.N * c.B * 2 * split_layout(c.B).BH; };
     for (auto& c : g->cls) {
         total += 2 * rnd(sizeof(int64_t) * c.N);
-        total += rnd(sizeof(float) * 2 * (size_t)c.N * c.B * 2 * c.B) + rnd(sizeof(float) * 2 * (size_t)c.N * c.B * c.B);
+        total += rnd(sizeof(float) * x_floats(c)) + rnd(sizeof(float) * c_floats(c));
     }
     if (r == S2G_OK && cudaMalloc(&g->mem, total) != cudaSuccess)
         r = fail(S2G_ERR_NOMEM, "group: cudaMalloc of %zu bytes failed", total);
@@ -469,9 +491,9 @@ int s2g_group_create(s2g_group* out, int nfunc, const int* bw, int precision) {
             c.cmap = (int64_t*)p;
             p += rnd(sizeof(int64_t) * c.N);
             c.buf0 = (float*)p;
-            p += rnd(sizeof(float) * 2 * (size_t)c.N * c.B * 2 * c.B);
+            p += rnd(sizeof(float) * x_floats(c));
             c.buf1 = (float*)p;
-            p += rnd(sizeof(float) * 2 * (size_t)c.N * c.B * c.B);
+            p += rnd(sizeof(float) * c_floats(c));
             gm.clear();
             cm.clear();
             for (int f : c.funcs) gm.push_back(g->goff[f]), cm.push_back(g->coff[f]);

@@ -202,6 +202,8 @@ struct StageSpec {
     const int64_t* gmap;
 };
 int split_stage_group(int which, const StageSpec* spec, int ncls, int dct_ctas_per_sm, cudaStream_t st);
+// The same stage for one class of any split-path bandwidth, as its own launch.
+int split_stage_one(int which, Tables* t, int N, const void* in, void* out, const int64_t* gmap, cudaStream_t st);
 // Reads (and optionally clears) the device error word of the tensor-core kernels.
 int split_device_status(Tables* t, int clear);
 

@@ -1003,7 +1003,7 @@ __global__ void __launch_bounds__(256, StageOcc<WHICH, RMAX>::v) k_stage_group(c
 // FP16 terms (S2G_PREC_FP16X2): each A row is scaled by a power of two 2^e_r chosen from the
 // row's largest magnitude (|x| 2^e_r < 2^14) and the table blob by one power of two per
 // bandwidth, so that FP16's exponent range holds both; the epilogue undoes both scales.
-static constexpr int kMaxClasses = 6;  // bandwidths 16 .. 512
+static constexpr int kMaxClasses = 16;  // bandwidth classes of one contraction launch
 
 struct LegClass {
     int B, N, ntiles;         // bandwidth, functions, 64-function tiles
@@ -2839,6 +2839,17 @@ int inv_fst_split_complex(Tables* t, const float* rc, const float* ic, float* rg
     }
     S2G_TRY(inv_fst_split(t, g, g + n, rgrid, batch, precision, work, st));
     return inv_fst_split(t, h, h + n, igrid, batch, precision, work, st);
+}
+
+// One FFT stage of one bandwidth class on its own launch (the per-length warp-FFT or chirp-z
+// kernels), with the scale of that stage; in/out and gmap as split_stage_group.
+int split_stage_one(int which, Tables* t, int N, const void* in, void* out, const int64_t* gmap, cudaStream_t st) {
+    if (which < 0 || which > 3) return fail(S2G_ERR_ARG, "stage %d", which);
+    S2G_TRY(build_split(t));
+    const Split* s = (const Split*)t->split;
+    const int B = t->bw, S = 2 * B;
+    const float scale = which == 0 ? (float)(sqrt(2.0 * kPi) / S) : which == 2 ? (float)(1.0 / sqrt(2.0 * kPi)) : 1.f;
+    return fft_kernels(which, B, in, out, N, s, st, scale, (which == 0 || which == 3) ? gmap : nullptr);
 }
 
 // Inverse stages after the contraction: REDFT01 (+ sin(theta) for odd m), naive-order

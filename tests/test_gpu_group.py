@@ -70,9 +70,12 @@ def _gather(g, flat, idx, size, offsets):
 
 
 @pytest.mark.parametrize("prec", [api.PREC_FP16X2, api.PREC_BF16X3])
-def test_group_equals_uniform_path_bitwise(prec):
+@pytest.mark.parametrize("bws", [[16, 32, 16, 64, 128, 32, 256, 16, 64, 32, 128, 16],
+                                 # any split-path bandwidth: warp-FFT lengths 32 R with R not a power of
+                                 # two (48, 192) and chirp-z lengths (17, 33, 100, 127, 255) beside powers of two
+                                 [17, 48, 100, 127, 192, 255, 64, 17, 100, 33, 16, 256]])
+def test_group_equals_uniform_path_bitwise(prec, bws):
     torch = _torch()
-    bws = [16, 32, 16, 64, 128, 32, 256, 16, 64, 32, 128, 16]
     ref = _fp64_reference(bws, 2.0, 7)
     g = api.Group(bws, prec)
     grid, rc, ic = _pack(g, ref)
@@ -191,7 +194,9 @@ def test_group_stage_launches_do_not_grow_with_classes():
 
 def test_group_rejects_bad_arguments():
     with pytest.raises(S2GError):
-        api.Group([16, 48], api.PREC_FP16X2)
+        api.Group([16, 300], api.PREC_FP16X2)  # above 256 and not a power of two
+    with pytest.raises(S2GError):
+        api.Group(list(range(16, 33)), api.PREC_FP16X2)  # 17 distinct bandwidths
     with pytest.raises(S2GError):
         api.Group([16, 32], api.PREC_FP64)
     with pytest.raises(S2GError):
