@@ -295,7 +295,8 @@ class Plan:
 class Group:
     """Grouped transforms of many real functions of uneven bandwidth (s2g_group_*).
 
-    ``bws``: bandwidth of each function (powers of two in [16, 512]).  Device buffers are flat
+    ``bws``: bandwidth of each function (16 .. 256, or a power of two up to 512; at most 16
+    distinct bandwidths).  Device buffers are flat
     float32 tensors: the grid holds the functions' (2 bw)^2 samples back to back, rcoeffs/icoeffs
     their bw^2 coefficients; ``grid_offsets``/``coeff_offsets`` give each function's start.
     """

@@ -2,6 +2,8 @@
 // contraction on the 5th-generation tensor cores as split-BF16 products (FP32 accumulation in TMEM).
 //
 // Forward (FSTSemiMemo, REAL, cutoff = bw; FST_semi_memo.c:68-145):
+//   (the FFT stages below run as chirp-z transforms, czt_split.cu, at lengths 2 bw the warp FFTs
+//   do not take; the intermediate layout is then split_layout's padded one)
 //   k_rows_fwd_w       : DFT along phi (warp FFT, two real latitudes per warp), X[p][f][m][theta]
 //   k_dct_fwd_w        : weights (even/odd order) + REDFT10 + normalisation (seminaive.c:161-176)
 //                        -> C[p][f][m][t][j], cosine frequency k = 2j + t (parity-split)
