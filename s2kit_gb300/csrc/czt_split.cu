@@ -100,21 +100,25 @@ __device__ __forceinline__ void czt_warp(float2 (&v)[RM], const CztSm& t, float*
         q.y *= -sign;
         v[k1] = cmulf(v[k1], q);
     }
-    // to natural order through the warp's rows
-    __syncwarp();
+    // to natural order through the warp's rows.  At RM = 32 the four-step FFT's output order is
+    // its input order already (one lane per column: register s of lane L holds index L + 32 s),
+    // so the product goes straight into the second FFT.
+    if constexpr (RM != 32) {
+        __syncwarp();
 #pragma unroll
-    for (int k1 = 0; k1 < RM; ++k1) {
-        const int o = pad32(WarpFFTSel<RM>::out_index(k1));
-        zr[o] = v[k1].x;
-        zi[o] = v[k1].y;
-    }
-    __syncwarp();
+        for (int k1 = 0; k1 < RM; ++k1) {
+            const int o = pad32(WarpFFTSel<RM>::out_index(k1));
+            zr[o] = v[k1].x;
+            zi[o] = v[k1].y;
+        }
+        __syncwarp();
 #pragma unroll
-    for (int i = 0; i < RM; ++i) {
-        const int o = pad32(lane + 32 * i);
-        v[i] = make_float2(zr[o], zi[o]);
+        for (int i = 0; i < RM; ++i) {
+            const int o = pad32(lane + 32 * i);
+            v[i] = make_float2(zr[o], zi[o]);
+        }
+        __syncwarp();
     }
-    __syncwarp();
     WarpFFTSel<RM>::run(v, t.tw, t.twb, zr, zi, 1.f);  // M IDFT_M (the 1/M is in the kernel spectrum)
     __syncwarp();
 #pragma unroll
