@@ -48,8 +48,9 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--group", type=int, default=1, help="also time the grouped uneven-bandwidth workload")
-    ap.add_argument("--phase", default="all", choices=["all", "split"],
-                    help="split: only the warm-up and timed device-resident split steps (for profilers)")
+    ap.add_argument("--phase", default="all", choices=["all", "split", "group"],
+                    help="split: only the warm-up and timed device-resident split steps (for profilers); "
+                         "group: only the grouped uneven-bandwidth workload")
     return ap.parse_args()
 
 
@@ -251,6 +252,14 @@ def main():
             dist.barrier()
 
     lib = load()
+    if args.phase == "group":  # the grouped uneven-bandwidth workload alone (config 4), for profiling
+        if rank == 0:
+            grp = group_bench(api, torch, torch.cuda.current_stream(), args.steps, args.warmup, args.seed)
+            print(json.dumps({"phase": "group", **{k: grp[k] for k in ("workload", "value", "unit", "ms_per_step",
+                                                                      "graph_kernels", "tiles")}}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     B, N = args.bw, args.batch
     S = 2 * B
     rng = np.random.default_rng(args.seed + rank)
